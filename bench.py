@@ -1,0 +1,371 @@
+"""Benchmark: the Plenoxels training step at scale (256^3 grid, 20% occupancy,
+SH degree 2, 1,000,000 rays per step) on GB300.
+
+One step = volume_render_fused (ray march + MSE adjoint, gradients scattered
+into the grid) + inplace_tv_grad on density (lambda 1e-5) and on SH (1e-3),
+1% contiguous cell window each + RMSprop on density (lr 30) and SH (lr 1e-2),
+beta 0.95 — the order of the reference's training loop (opt/opt.py:499-595).
+Inputs are seeded synthetic data with the configuration's distributions
+(svox2_gb300/synthetic.py); the grid and its gradient/RMS state (1.2 GB)
+exceed the 129 MB L2, so no flush is needed between steps.
+
+Prints ONE JSON line.  `value` = rays/s with rays already in HBM; `e2e` =
+the same step through the public SparseGrid API with each step's rays copied
+from pinned host memory and the rendered colours copied back.  `roofline` is
+for the fused render kernel (the dominant kernel): algorithmic bytes =
+3648 B per evaluated sample (8 corners x (link + density + 27 SH) gathered
+twice + 8 x 28 float gradients read-modify-written) + 48 B per ray.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference algorithm's CPU restatement (oracle/,
+all host threads) on a bounded sample of the same step.
+N > 1 (torchrun): independent replicas, one per GPU (the path has no
+exchange step); value = total rays / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+import torch
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+RESO = 256
+OCC = 0.20
+N_BALLS = 8
+Q = 1_000_000
+BYTES_PER_SAMPLE = 3648
+BYTES_PER_RAY = 48
+METRIC = "fused fwd+bwd rays/s at 256^3 SH9 (train step: render+MSE adjoint, TV, RMSprop)"
+WORKLOAD = "train step 256^3 20% occupancy SH9 FP32, 1M rays/step, fused fwd+bwd + TV + RMSprop"
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.thread.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def build_workload(device, seed_rays: int, n_batches: int):
+    from svox2_gb300 import synthetic as S
+    from svox2_gb300 import SparseGrid
+
+    g = S.make_grid(RESO, occupancy=OCC, n_balls=N_BALLS, seed=0, device=device)
+    grid = SparseGrid(reso=RESO, basis_dim=9, device=device)
+    N = g.density.shape[0]
+    grid.links = g.links.to(device)
+    grid.density_data = torch.nn.Parameter(g.density.to(device))
+    grid.sh_data = torch.nn.Parameter(g.sh.to(device))
+    grid.capacity = N
+    grid.opt.sigma_thresh = 1e-8
+    grid.opt.stop_thresh = 1e-7
+    grid.opt.background_brightness = 1.0
+    grid.opt.step_size = 0.5
+    batches = [S.make_rays(Q, seed=seed_rays + i) for i in range(n_batches)]
+    return g, grid, batches
+
+
+def train_step(grid, rays_o, rays_d, gt, stats=None, ev=None):
+    """One step of the training loop; ev = (start, stop) events bracketing the fused render."""
+    from svox2_gb300 import Rays
+    from svox2_gb300 import csrc as C
+
+    if stats is None and ev is None:
+        rgb = grid.volume_render_fused(Rays(rays_o, rays_d), gt)
+    else:
+        gd, gs = grid._get_data_grads()
+        rgb = torch.empty_like(gt)
+        grid.sparse_grad_indexer = torch.zeros((grid.density_data.size(0),), dtype=torch.bool,
+                                               device=gt.device)
+        holder = C.GridOutputGrads()
+        holder.grad_density_out = gd
+        holder.grad_sh_out = gs
+        holder.mask_out = grid.sparse_grad_indexer
+        r = C.RaysSpec()
+        r.origins, r.dirs = rays_o, rays_d
+        if ev is not None:
+            ev[0].record()
+        C.volume_render_cuvol_fused(grid._to_cpp(), r, grid.opt._to_cpp(), gt, 0.0, 0.0, rgb, holder, stats=stats)
+        if ev is not None:
+            ev[1].record()
+        grid.sparse_sh_grad_indexer = grid.sparse_grad_indexer.clone()
+    grid.inplace_tv_grad(grid.density_data.grad, scaling=1e-5, sparse_frac=0.01, contiguous=True)
+    grid.inplace_tv_color_grad(grid.sh_data.grad, scaling=1e-3, sparse_frac=0.01, contiguous=True)
+    grid.optim_density_step(30.0, beta=0.95, epsilon=1e-8)
+    grid.optim_sh_step(1e-2, beta=0.95, epsilon=1e-8)
+    return rgb
+
+
+def cpu_sample(g, budget_s: float = 12.0, threads: int | None = None):
+    """The oracle's fused fwd+bwd on a bounded sample of the same workload, plus the
+    TV + RMSprop work on a proportional slice of the grid.  Returns (rays/s, cores, desc)."""
+    from oracle import oracle as O
+    from svox2_gb300 import synthetic as S
+
+    threads = threads or (os.cpu_count() or 1)
+    off, scl = S.grid_transform(g.reso)
+    og = O.Grid(g.links.numpy(), g.density.numpy(), g.sh.numpy(), 9, off, scl)
+    opt = O.Opt(1.0, 0.5, 1e-8, 1e-7)
+    N = g.density.shape[0]
+
+    def step(n):
+        o, d, gt = S.make_rays(n, seed=12345)
+        t0 = time.perf_counter()
+        r = O.render(og, opt, o.numpy(), d.numpy(), mode=1, rgb_gt=gt.numpy(), nthreads=threads)
+        rows = max(int(N * n / Q), 1)
+        dd = g.density.numpy()[:rows]
+        O.optim(True, dd, np.zeros_like(dd), r["grad_density"][:rows].astype(np.float32), 2, r["mask"][:rows])
+        ss = g.sh.numpy()[:rows]
+        O.optim(True, ss, np.zeros_like(ss), r["grad_sh"][:rows].astype(np.float32), 2, r["mask"][:rows])
+        cells = max(int(0.01 * g.links.numel() * n / Q), 1)
+        cl = np.arange(cells, dtype=np.int32) + g.links.numel() // 3
+        O.tv_grad(g.links.numpy(), g.density.numpy(), 0, 1, 1e-5, False, cells=cl)
+        O.tv_grad(g.links.numpy(), g.sh.numpy(), 0, 27, 1e-3, True, cells=cl)
+        return time.perf_counter() - t0
+
+    n = 512
+    t = step(n)
+    n = int(max(512, min(1 << 20, n * budget_s / max(t, 1e-3))))
+    t = step(n)
+    return n / t, threads, f"{n} rays of the 256^3 workload fused fwd+bwd + TV/RMSprop on {n}/{Q} of the grid"
+
+
+def run_reference(args, rank, world):
+    """Reference arm: the CPU restatement of the reference algorithm, all host threads."""
+    if rank != 0:
+        return
+    from svox2_gb300 import synthetic as S
+
+    g = S.make_grid(RESO, occupancy=OCC, n_balls=N_BALLS, seed=0)
+    # size each step to ~1 s so that warmup + steps ends within a few minutes
+    per_step_s = min(1.0, 150.0 / max(args.steps + args.warmup, 1))
+    rate, cores, _ = cpu_sample(g, budget_s=per_step_s)
+    n = max(256, int(rate * per_step_s))
+    from oracle import oracle as O
+
+    off, scl = S.grid_transform(g.reso)
+    og = O.Grid(g.links.numpy(), g.density.numpy(), g.sh.numpy(), 9, off, scl)
+    opt = O.Opt(1.0, 0.5, 1e-8, 1e-7)
+    times = []
+    for i in range(args.warmup + args.steps):
+        o, d, gt = S.make_rays(n, seed=100 + i)
+        t0 = time.perf_counter()
+        O.render(og, opt, o.numpy(), d.numpy(), mode=1, rgb_gt=gt.numpy(), nthreads=cores)
+        if i >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    tot = sum(times)
+    val = n * len(times) / tot
+    line = {
+        "metric": METRIC, "value": val, "unit": "rays/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * Q / val, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic", "impl": "reference",
+        "config": {"workload": WORKLOAD, "reso": RESO, "occupancy": OCC, "rays_per_step": Q},
+        "cpu_baseline": {"value": val, "unit": "rays/s", "cores": cores, "kind": "port",
+                         "sample": f"{n} rays per step, fused fwd+bwd of the 256^3 workload (CPU restatement)"},
+        "e2e": {"value": val, "unit": "rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+
+        dist = dist_mod
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+
+    device = torch.device("cuda", local)
+    torch.cuda.set_device(device)
+    import __graft_entry__ as ge  # noqa: F401  (path setup)
+    from svox2_gb300 import Rays
+
+    n_batches = min(args.steps + args.warmup, 8)
+    g, grid, host_batches = build_workload(device, seed_rays=1000 + 97 * rank, n_batches=n_batches)
+    dev_batches = [tuple(t.to(device) for t in b) for b in host_batches]
+    stats = {"eval_samples": torch.zeros(1, dtype=torch.int64, device=device)}
+
+    # ---- warmup
+    for i in range(args.warmup):
+        o, d, gt = dev_batches[i % n_batches]
+        train_step(grid, o, d, gt)
+    torch.cuda.synchronize()
+
+    # ---- timed: device-resident inputs
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    t_start, t_stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stats["eval_samples"].zero_()
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(device.index if device.index is not None else 0) as clk:
+        t_start.record()
+        for i in range(args.steps):
+            o, d, gt = dev_batches[i % n_batches]
+            train_step(grid, o, d, gt, stats=stats, ev=evs[i])
+        t_stop.record()
+        torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    total_ms = t_start.elapsed_time(t_stop)
+    kern_ms = sum(a.elapsed_time(b) for a, b in evs)
+    n_eval = int(stats["eval_samples"].item())
+    if dist is not None:
+        tt = torch.tensor([total_ms], device=device)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_ms = float(tt.item())
+
+    # ---- e2e: public API, rays from pinned host memory, colours back to the host
+    pinned = [tuple(t.pin_memory() for t in b) for b in host_batches]
+    dbuf = tuple(torch.empty((Q, 3), device=device) for _ in range(3))
+    hout = torch.empty((Q, 3), dtype=torch.float32).pin_memory()
+    for i in range(args.warmup):
+        for dst, src in zip(dbuf, pinned[i % n_batches]):
+            dst.copy_(src, non_blocking=True)
+        rgb = train_step(grid, *dbuf)
+        hout.copy_(rgb, non_blocking=True)
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    e_start, e_stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e_start.record()
+    for i in range(args.steps):
+        for dst, src in zip(dbuf, pinned[i % n_batches]):
+            dst.copy_(src, non_blocking=True)
+        rgb = train_step(grid, *dbuf)
+        hout.copy_(rgb, non_blocking=True)
+    e_stop.record()
+    torch.cuda.synchronize()
+    e2e_ms = e_start.elapsed_time(e_stop)
+    if dist is not None:
+        tt = torch.tensor([e2e_ms], device=device)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_ms = float(tt.item())
+
+    value = world * Q * args.steps / (total_ms / 1e3)
+    e2e_val = world * Q * args.steps / (e2e_ms / 1e3)
+    peak, peak_kind = _peaks()
+    per_launch_s = kern_ms / 1e3 / args.steps
+    alg_bytes = (n_eval / args.steps) * BYTES_PER_SAMPLE + BYTES_PER_RAY * Q
+    achieved = alg_bytes / per_launch_s / 1e9
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        rate, cores, desc = cpu_sample(g)
+        cpu = {"value": rate, "unit": "rays/s", "cores": cores, "kind": "port", "sample": desc}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "reso": RESO, "occupancy": float(g.occupancy), "n_voxels": int(
+                g.density.shape[0]), "rays_per_step": Q, "l2": "no flush: grid + grads + RMS state 1.2 GB > L2",
+                "parallelism": f"replicas x{world}"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                         "kernel": "render_kernel<9,float,fused>", "kernel_ms": kern_ms / args.steps,
+                         "eval_samples_per_step": n_eval / args.steps},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_val, "unit": "rays/s", "h2d_bytes_per_step": 3 * Q * 3 * 4,
+                    "d2h_bytes_per_step": Q * 3 * 4},
+            "gpu_launches": 5 * args.steps,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,247 @@
+/*
+ * svox2_gb300 — C ABI of the GB300-native (sm_103a) Plenoxels sparse-voxel renderer.
+ *
+ * Every entry point takes plain pointers and sizes, never a framework tensor.
+ * All data pointers are DEVICE pointers on the current CUDA device unless a
+ * field says otherwise; `stream` is a cudaStream_t passed as void* (NULL = the
+ * legacy default stream).  Every call is asynchronous on `stream`, returns an
+ * svx_status (0 = success) and leaves a one-line message for
+ * svx_last_error() on failure (thread-local).  Kernel launches are checked
+ * with cudaGetLastError; faults inside a kernel surface at the caller's next
+ * synchronisation.
+ *
+ * Each function replaces one operator of the reference's `svox2.csrc`
+ * extension (pybind11 table in svox2/csrc/svox2.cpp:74-112); the comment above
+ * each declaration names the reference declaration and implementation it
+ * stands in for.  Argument meaning follows the reference; where the reference
+ * passed a torch::Tensor, the ABI passes its device pointer plus the sizes the
+ * reference read from the tensor.
+ */
+#ifndef SVOX2_GB300_H_
+#define SVOX2_GB300_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SVX_ABI_VERSION 1
+
+/* Status codes.  The reference raised RuntimeError through TORCH_CHECK
+ * (svox2/csrc/include/data_spec.hpp:32-51); the ABI returns these instead and
+ * the Python layer raises RuntimeError with svx_last_error(). */
+typedef enum {
+  SVX_OK = 0,
+  SVX_ERR_INVALID = 1,      /* bad argument: null pointer, size, dtype, range */
+  SVX_ERR_UNSUPPORTED = 2,  /* feature outside this build (MSI background, MLP basis…) */
+  SVX_ERR_CUDA = 3,         /* a CUDA runtime call or kernel launch failed */
+  SVX_ERR_TOO_LARGE = 4     /* size beyond a documented limit */
+} svx_status;
+
+/* Storage type of a float table (SH coefficients, TV/optimiser data). */
+typedef enum { SVX_F32 = 0, SVX_BF16 = 1, SVX_F16 = 2 } svx_dtype;
+
+/* Basis types, svox2/defs.py:1-4.  Only SVX_BASIS_SH is built. */
+#define SVX_BASIS_SH 1
+#define SVX_BASIS_3D_TEXTURE 4
+#define SVX_BASIS_MLP 255
+
+/* Grid description — SparseGridSpec, svox2/csrc/include/data_spec.hpp:18-52,
+ * packed form svox2/csrc/include/data_spec_packed.cuh:11-62.
+ *   links      int32 [size0, size1, size2], C-contiguous; >= 0 is a row index
+ *              into the data tables, -1 is empty, < -1 is an empty-space skip
+ *              level written by accel_dist_prop.
+ *   density    float32 [n_voxels, 1].
+ *   sh         [n_voxels, sh_data_dim] of sh_dtype, channel-major per voxel:
+ *              coefficient k of colour channel c is sh[v, c*basis_dim + k].
+ *   offset/scaling  world -> grid transform, grid = world*scaling + offset
+ *              (the reference's _offset/_scaling CPU tensors, svox2/svox2.py:2135-2161).
+ *   background_nlayers  must be 0 (the MSI background model is not built). */
+typedef struct {
+  const float* density_data;
+  const void* sh_data;
+  const int32_t* links;
+  int64_t n_voxels;
+  int32_t size[3];
+  int32_t basis_dim;
+  int32_t sh_data_dim;
+  int32_t basis_type;
+  int32_t sh_dtype;
+  int32_t background_nlayers;
+  float offset[3];
+  float scaling[3];
+} svx_grid_t;
+
+/* RaysSpec, data_spec.hpp:104-113: origins and unit directions, float32 [n_rays, 3]. */
+typedef struct {
+  const float* origins;
+  const float* dirs;
+  int64_t n_rays;
+} svx_rays_t;
+
+/* CameraSpec, data_spec.hpp:83-102.  c2w is a DEVICE float32 row-major matrix
+ * with 4 columns and c2w_rows (3 or 4) rows, OpenCV convention. */
+typedef struct {
+  const float* c2w;
+  int32_t c2w_rows;
+  float fx, fy, cx, cy;
+  int32_t width, height;
+  float ndc_coeffx, ndc_coeffy;
+} svx_camera_t;
+
+/* RenderOptions, data_spec.hpp:115-135. */
+typedef struct {
+  float background_brightness;
+  float step_size;
+  float sigma_thresh;
+  float stop_thresh;
+  float near_clip;
+  int32_t use_spheric_clip;
+  int32_t last_sample_opaque;
+} svx_render_opts_t;
+
+/* GridOutputGrads, data_spec.hpp:54-81.  Gradients are float32 and are
+ * ACCUMULATED into (not overwritten).  mask_out (bool/uint8 [n_voxels]) may be
+ * NULL; when given, every voxel that received a gradient is set to 1. */
+typedef struct {
+  float* grad_density_out;
+  float* grad_sh_out;
+  uint8_t* mask_out;
+} svx_grid_grads_t;
+
+/* Optional instrumentation for the render entry points (may be NULL):
+ *   eval_samples  device uint64 accumulator: += number of evaluated samples
+ *                 (sigma > sigma_thresh, before early stop) over the launch.
+ *   ray_trace     device uint64 [n_rays]: per-ray hash of the sequence of
+ *                 (cell, links, evaluated) decisions; lets tests compare the
+ *                 sample indexing bit for bit with a CPU restatement. */
+typedef struct {
+  uint64_t* eval_samples;
+  uint64_t* ray_trace;
+} svx_render_stats_t;
+
+/* ---- rendering: svox2/csrc/render_lerp_kernel_cuvol.cu ---------------- */
+
+/* volume_render_cuvol (svox2/csrc/svox2.cpp:18, render_lerp_kernel_cuvol.cu:918-958).
+ * rgb_out float32 [n_rays, 3]. */
+int svx_volume_render_cuvol(const svx_grid_t* grid, const svx_rays_t* rays,
+                            const svx_render_opts_t* opt, float* rgb_out,
+                            const svx_render_stats_t* stats, void* stream);
+
+/* volume_render_cuvol_image (svox2/csrc/svox2.cpp:19-20, render_lerp_kernel_cuvol.cu:960-1008).
+ * rgb_out float32 [height, width, 3]. */
+int svx_volume_render_cuvol_image(const svx_grid_t* grid, const svx_camera_t* cam,
+                                  const svx_render_opts_t* opt, float* rgb_out,
+                                  const svx_render_stats_t* stats, void* stream);
+
+/* volume_render_cuvol_backward (svox2/csrc/svox2.cpp:21-22, render_lerp_kernel_cuvol.cu:1010-1068).
+ * grad_out = dL/d(rgb) float32 [n_rays, 3].  color_cache is the forward
+ * output; it is accepted for interface parity and may be NULL, because this
+ * adjoint rebuilds what it needs from the grid.  Gradients accumulate into
+ * grads; the reference does not set the mask on this path, neither does this. */
+int svx_volume_render_cuvol_backward(const svx_grid_t* grid, const svx_rays_t* rays,
+                                     const svx_render_opts_t* opt, const float* grad_out,
+                                     const float* color_cache, const svx_grid_grads_t* grads,
+                                     const svx_render_stats_t* stats, void* stream);
+
+/* volume_render_cuvol_fused (svox2/csrc/svox2.cpp:23-24, render_lerp_kernel_cuvol.cu:1070-1152).
+ * Renders rgb_out [n_rays,3] and accumulates the gradient of
+ * mean((rgb_out - rgb_gt)^2) (+ beta_loss, sparsity_loss terms) into grads,
+ * setting grads->mask_out for every touched voxel. */
+int svx_volume_render_cuvol_fused(const svx_grid_t* grid, const svx_rays_t* rays,
+                                  const svx_render_opts_t* opt, const float* rgb_gt,
+                                  float beta_loss, float sparsity_loss, float* rgb_out,
+                                  const svx_grid_grads_t* grads,
+                                  const svx_render_stats_t* stats, void* stream);
+
+/* ---- point sampling: svox2/csrc/svox2_kernel.cu ------------------------ */
+
+/* sample_grid (svox2/csrc/svox2.cpp:11-12, svox2_kernel.cu:181-217).
+ * points float32 [n_points, 3] in world coordinates (grid->offset/scaling
+ * apply).  out_density float32 [n_points, 1]; out_sh float32
+ * [n_points, sh_data_dim], written only when want_colors != 0. */
+int svx_sample_grid(const svx_grid_t* grid, const float* points, int64_t n_points,
+                    int32_t want_colors, float* out_density, float* out_sh, void* stream);
+
+/* sample_grid_backward (svox2/csrc/svox2.cpp:13-14, svox2_kernel.cu:219-267).
+ * Accumulates into grad_density_out [n_voxels,1] and (want_colors)
+ * grad_sh_out [n_voxels, sh_data_dim]. */
+int svx_sample_grid_backward(const svx_grid_t* grid, const float* points, int64_t n_points,
+                             const float* grad_out_density, const float* grad_out_sh,
+                             float* grad_density_out, float* grad_sh_out,
+                             int32_t want_colors, void* stream);
+
+/* ---- total variation: svox2/csrc/loss_kernel.cu ------------------------ */
+
+/* A float table [n_rows, n_cols] of data_dtype (density or SH). */
+typedef struct {
+  const void* data;
+  int32_t dtype;
+  int64_t n_rows;
+  int32_t n_cols;
+} svx_table_t;
+
+/* tv_grad (svox2/csrc/svox2.cpp:62-63, loss_kernel.cu:111-176, host 522-556).
+ * Dense TV gradient over all (size0-1)(size1-1)(size2-1) cells, channels
+ * [start_dim, end_dim), scaled by scale / n_cells, accumulated into grad
+ * (float32 [n_rows, n_cols]).  use_logalpha/logalpha_delta are accepted and
+ * unused, as in the reference. */
+int svx_tv_grad(const int32_t* links, const int32_t size[3], const svx_table_t* data,
+                int32_t start_dim, int32_t end_dim, float scale, int32_t use_logalpha,
+                float logalpha_delta, int32_t ignore_edge, float ndc_coeffx,
+                float ndc_coeffy, float* grad, void* stream);
+
+/* tv_grad_sparse (svox2/csrc/svox2.cpp:64-65, loss_kernel.cu:178-246, host 558-604).
+ * TV gradient on the n_cells linear cell indices rand_cells (int32), scaled
+ * by scale / n_cells; sets mask_out[v] = 1 for every voxel written (mask_out
+ * may be NULL). */
+int svx_tv_grad_sparse(const int32_t* links, const int32_t size[3], const svx_table_t* data,
+                       const int32_t* rand_cells, int64_t n_cells, uint8_t* mask_out,
+                       int32_t start_dim, int32_t end_dim, float scale, int32_t use_logalpha,
+                       float logalpha_delta, int32_t ignore_edge, int32_t ignore_last_z,
+                       float ndc_coeffx, float ndc_coeffy, float* grad, void* stream);
+
+/* ---- optimisers: svox2/csrc/optim_kernel.cu ---------------------------- */
+
+/* How the optimiser selects rows: the reference dispatched on the indexer
+ * tensor (optim_kernel.cu:168-216): 0-dim -> all rows, empty -> nothing,
+ * bool [n_rows] -> mask, int64 [n] -> row list. */
+typedef enum {
+  SVX_INDEX_ALL = 0,
+  SVX_INDEX_NONE = 1,
+  SVX_INDEX_MASK = 2,   /* indexer: const uint8_t* [n_rows] */
+  SVX_INDEX_LIST = 3    /* indexer: const int64_t* [n_index] */
+} svx_indexer_kind;
+
+/* rmsprop_step (svox2/csrc/svox2.cpp:70-71, optim_kernel.cu:154-218).
+ * data [n_rows, n_cols] of data_dtype (updated in place; f32, bf16 or f16),
+ * rms and grad float32 [n_rows, n_cols]; grad is zeroed on the visited rows.
+ * lr_last < 0 means lr_last = lr.  The last column uses lr_last. */
+int svx_rmsprop_step(void* data, int32_t data_dtype, float* rms, float* grad,
+                     int64_t n_rows, int32_t n_cols, int32_t indexer_kind,
+                     const void* indexer, int64_t n_index, float beta, float lr,
+                     float epsilon, float minval, float lr_last, void* stream);
+
+/* sgd_step (svox2/csrc/svox2.cpp:72, optim_kernel.cu:220-267). */
+int svx_sgd_step(void* data, int32_t data_dtype, float* grad, int64_t n_rows,
+                 int32_t n_cols, int32_t indexer_kind, const void* indexer,
+                 int64_t n_index, float lr, float lr_last, void* stream);
+
+/* ---- library ------------------------------------------------------------ */
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* svx_last_error(void);
+
+/* SVX_ABI_VERSION of the loaded library. */
+int svx_abi_version(void);
+
+/* Largest number of evaluated samples per ray whose colours the fused
+ * adjoint keeps on chip; samples past it are re-gathered in the reverse pass. */
+int svx_color_cache_capacity(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SVOX2_GB300_H_ */

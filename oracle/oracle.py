@@ -1,0 +1,212 @@
+"""numpy front end of the CPU oracle (liboracle.so) — TEST INFRASTRUCTURE.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU arms import this
+module; the svox2_gb300 product never does.  Every function takes numpy
+arrays (float32 grid tables, int32 links, float32 rays) and returns numpy
+results in the requested precision ("f32" = the reference's float arithmetic,
+"f64" = the double-precision yardstick).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+from typing import Optional
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+
+
+class OGrid(C.Structure):
+    _fields_ = [("links", C.c_void_p), ("density", C.c_void_p), ("sh", C.c_void_p), ("n_voxels", C.c_int64),
+                ("size", C.c_int * 3), ("basis_dim", C.c_int), ("offset", C.c_float * 3),
+                ("scaling", C.c_float * 3)]
+
+
+class OOpt(C.Structure):
+    _fields_ = [("bg", C.c_float), ("step", C.c_float), ("sigma_thresh", C.c_float), ("stop_thresh", C.c_float),
+                ("near_clip", C.c_float), ("spheric", C.c_int), ("last_opaque", C.c_int)]
+
+
+class OCam(C.Structure):
+    _fields_ = [("c2w", C.c_void_p), ("fx", C.c_float), ("fy", C.c_float), ("cx", C.c_float), ("cy", C.c_float),
+                ("width", C.c_int), ("height", C.c_int), ("ndcx", C.c_float), ("ndcy", C.c_float)]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(str(_build.build()))
+    return _lib
+
+
+@dataclass
+class Grid:
+    """Grid tables in the reference layout (numpy, float32 / int32)."""
+    links: np.ndarray          # int32 [X, Y, Z]
+    density: np.ndarray        # float32 [N, 1] or [N]
+    sh: np.ndarray             # float32 [N, 3*bd]
+    basis_dim: int
+    offset: tuple              # grid = world * scaling + offset (the reference's _to_cpp transform)
+    scaling: tuple
+
+    def struct(self) -> OGrid:
+        self.links = np.ascontiguousarray(self.links, dtype=np.int32)
+        self.density = np.ascontiguousarray(self.density, dtype=np.float32)
+        self.sh = np.ascontiguousarray(self.sh, dtype=np.float32)
+        g = OGrid()
+        g.links = self.links.ctypes.data
+        g.density = self.density.ctypes.data
+        g.sh = self.sh.ctypes.data
+        g.n_voxels = self.density.shape[0]
+        g.size = (C.c_int * 3)(*self.links.shape)
+        g.basis_dim = self.basis_dim
+        g.offset = (C.c_float * 3)(*[float(v) for v in self.offset])
+        g.scaling = (C.c_float * 3)(*[float(v) for v in self.scaling])
+        return g
+
+
+@dataclass
+class Opt:
+    background_brightness: float = 1.0
+    step_size: float = 0.5
+    sigma_thresh: float = 1e-10
+    stop_thresh: float = 1e-7
+    near_clip: float = 0.0
+    use_spheric_clip: bool = False
+    last_sample_opaque: bool = False
+
+    def struct(self) -> OOpt:
+        return OOpt(self.background_brightness, self.step_size, self.sigma_thresh, self.stop_thresh,
+                    self.near_clip, int(self.use_spheric_clip), int(self.last_sample_opaque))
+
+
+def _real(prec: str):
+    if prec not in ("f32", "f64"):
+        raise ValueError("prec must be 'f32' or 'f64'")
+    return np.float32 if prec == "f32" else np.float64
+
+
+def _p(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data
+
+
+def default_threads() -> int:
+    return int(os.environ.get("ORACLE_THREADS", os.cpu_count() or 1))
+
+
+def render(grid: Grid, opt: Opt, origins, dirs, mode: int = 0, rgb_gt=None, grad_out=None, color=None,
+           beta_loss: float = 0.0, sparsity_loss: float = 0.0, prec: str = "f32", want_grads: bool = True,
+           want_mask: bool = True, trace: bool = False, nthreads: Optional[int] = None) -> dict:
+    """volume_render_cuvol (mode 0), _fused (1), _backward (2, color = forward colour)."""
+    R = _real(prec)
+    origins = np.ascontiguousarray(origins, dtype=np.float32)
+    dirs = np.ascontiguousarray(dirs, dtype=np.float32)
+    Q = origins.shape[0]
+    N = grid.density.shape[0]
+    Cc = 3 * grid.basis_dim
+    rgb = np.zeros((Q, 3), dtype=R) if color is None else np.ascontiguousarray(color, dtype=R).copy()
+    gd = np.zeros((N, 1), dtype=R) if (mode and want_grads) else None
+    gs = np.zeros((N, Cc), dtype=R) if (mode and want_grads) else None
+    mask = np.zeros((N,), dtype=np.uint8) if (mode == 1 and want_mask) else None
+    tr = np.zeros((Q,), dtype=np.uint64) if trace else None
+    ne = np.zeros((1,), dtype=np.uint64)
+    gt = None if rgb_gt is None else np.ascontiguousarray(rgb_gt, dtype=np.float32)
+    go = None if grad_out is None else np.ascontiguousarray(grad_out, dtype=np.float32)
+    g = grid.struct()
+    o = opt.struct()
+    fn = getattr(lib(), "oracle_render_" + prec)
+    fn.restype = None
+    fn(C.byref(g), C.byref(o), C.c_void_p(_p(origins)), C.c_void_p(_p(dirs)), C.c_int64(Q), C.c_int(mode),
+       C.c_void_p(_p(gt)), C.c_void_p(_p(go)), C.c_float(beta_loss), C.c_float(sparsity_loss),
+       C.c_void_p(_p(rgb)), C.c_void_p(_p(gd)), C.c_void_p(_p(gs)), C.c_void_p(_p(mask)), C.c_void_p(_p(tr)),
+       C.c_void_p(_p(ne)), C.c_int(nthreads or default_threads()))
+    return {"rgb": rgb, "grad_density": gd, "grad_sh": gs, "mask": None if mask is None else mask.astype(bool),
+            "trace": tr, "n_eval": int(ne[0])}
+
+
+def render_image(grid: Grid, opt: Opt, c2w, fx, fy, cx, cy, width, height, ndc=(-1.0, -1.0), prec="f32",
+                 trace=False, nthreads=None) -> dict:
+    R = _real(prec)
+    c2w = np.ascontiguousarray(np.asarray(c2w, dtype=np.float32)[:3, :4])
+    cam = OCam(c2w.ctypes.data, fx, fy, cx, cy, width, height, ndc[0], ndc[1])
+    out = np.zeros((height, width, 3), dtype=R)
+    tr = np.zeros((height * width,), dtype=np.uint64) if trace else None
+    g = grid.struct()
+    o = opt.struct()
+    fn = getattr(lib(), "oracle_render_image_" + prec)
+    fn.restype = None
+    fn(C.byref(g), C.byref(o), C.byref(cam), C.c_void_p(out.ctypes.data), C.c_void_p(_p(tr)),
+       C.c_int(nthreads or default_threads()))
+    return {"rgb": out, "trace": tr}
+
+
+def sample(grid: Grid, points, want_colors=True, prec="f32"):
+    R = _real(prec)
+    pts = np.ascontiguousarray(points, dtype=np.float32)
+    P = pts.shape[0]
+    d = np.zeros((P, 1), dtype=R)
+    s = np.zeros((P, 3 * grid.basis_dim), dtype=R)
+    g = grid.struct()
+    fn = getattr(lib(), "oracle_sample_" + prec)
+    fn.restype = None
+    fn(C.byref(g), C.c_void_p(pts.ctypes.data), C.c_int64(P), C.c_int(int(want_colors)), C.c_void_p(d.ctypes.data),
+       C.c_void_p(s.ctypes.data))
+    return d, s
+
+
+def sample_backward(grid: Grid, points, grad_d, grad_sh, want_colors=True, prec="f32"):
+    R = _real(prec)
+    pts = np.ascontiguousarray(points, dtype=np.float32)
+    P = pts.shape[0]
+    gd_in = np.ascontiguousarray(grad_d, dtype=np.float32)
+    gs_in = np.ascontiguousarray(grad_sh, dtype=np.float32)
+    N = grid.density.shape[0]
+    od = np.zeros((N, 1), dtype=R)
+    os_ = np.zeros((N, 3 * grid.basis_dim), dtype=R)
+    g = grid.struct()
+    fn = getattr(lib(), "oracle_sample_backward_" + prec)
+    fn.restype = None
+    fn(C.byref(g), C.c_void_p(pts.ctypes.data), C.c_int64(P), C.c_int(int(want_colors)),
+       C.c_void_p(gd_in.ctypes.data), C.c_void_p(gs_in.ctypes.data), C.c_void_p(od.ctypes.data),
+       C.c_void_p(os_.ctypes.data))
+    return od, os_
+
+
+def tv_grad(links, data, start, end, scale, ignore_edge, cells=None, ignore_last_z=False, grad=None, mask=None,
+            prec="f32"):
+    """tv_grad (cells None) or tv_grad_sparse; accumulates into grad (returned) and mask."""
+    R = _real(prec)
+    links = np.ascontiguousarray(links, dtype=np.int32)
+    data = np.ascontiguousarray(data, dtype=np.float32)
+    grad = np.zeros(data.shape, dtype=R) if grad is None else grad
+    cl = None if cells is None else np.ascontiguousarray(cells, dtype=np.int32)
+    size = (C.c_int * 3)(*links.shape)
+    fn = getattr(lib(), "oracle_tv_grad_" + prec)
+    fn.restype = None
+    fn(C.c_void_p(links.ctypes.data), size, C.c_void_p(data.ctypes.data), C.c_int64(data.shape[0]),
+       C.c_int(data.shape[1]), C.c_void_p(_p(cl)), C.c_int64(0 if cl is None else cl.shape[0]), C.c_int(start),
+       C.c_int(end), C.c_float(scale), C.c_int(int(ignore_edge)), C.c_int(int(ignore_last_z)),
+       C.c_void_p(grad.ctypes.data), C.c_void_p(_p(mask)))
+    return grad
+
+
+def optim(rmsprop: bool, data, rms, grad, kind: int, indexer=None, beta=0.9, lr=1.0, eps=1e-8, minval=-1e9,
+          lr_last=-1.0, prec="f32"):
+    """rmsprop_step / sgd_step on copies; kind 0 all, 1 none, 2 mask, 3 index list."""
+    R = _real(prec)
+    data = np.ascontiguousarray(data, dtype=R).copy()
+    grad = np.ascontiguousarray(grad, dtype=R).copy()
+    rms = None if rms is None else np.ascontiguousarray(rms, dtype=R).copy()
+    mask = np.ascontiguousarray(indexer, dtype=np.uint8) if kind == 2 else None
+    index = np.ascontiguousarray(indexer, dtype=np.int64) if kind == 3 else None
+    fn = getattr(lib(), "oracle_optim_" + prec)
+    fn.restype = None
+    fn(C.c_int(int(rmsprop)), C.c_void_p(data.ctypes.data), C.c_void_p(_p(rms)), C.c_void_p(grad.ctypes.data),
+       C.c_int64(data.shape[0]), C.c_int(data.shape[1]), C.c_int(kind), C.c_void_p(_p(mask)),
+       C.c_void_p(_p(index)), C.c_int64(0 if index is None else index.shape[0]), C.c_float(beta), C.c_float(lr),
+       C.c_float(eps), C.c_float(minval), C.c_float(lr_last))
+    return data, rms, grad

@@ -1,0 +1,573 @@
+/*
+ * CPU restatement of the reference renderer's hot path — TEST INFRASTRUCTURE.
+ *
+ * This file is the ORACLE: it is only compiled into oracle/liboracle.so and is
+ * only used by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline and
+ * reference arms, to check or to time against.  Nothing in the svox2_gb300
+ * product links or calls it.
+ *
+ * It is included twice by svox2_oracle.c, with REAL = float (suffix _f32) and
+ * REAL = double (suffix _f64).  The float instance performs the reference
+ * kernels' IEEE operations in the reference's order (fmaf where the reference
+ * calls fmaf, no other contraction: it is built with -ffp-contract=off); the
+ * double instance is the same algorithm in double precision, the yardstick
+ * for every error statement.  Each function names the reference code it
+ * restates (paths inside the reference project).
+ *
+ * Two places where the reference's device code calls approximate hardware
+ * functions are restated from their mathematical definition:
+ *   - rnorm3df (svox2/csrc/include/cuda_util.cuh:87-92) -> 1/sqrt formed in double;
+ *   - the stop test __expf(logT) < stop_thresh (render_lerp_kernel_cuvol.cu:103,
+ *     370) -> logT < L with L the smallest REAL >= ln(stop_thresh), which is the
+ *     same predicate in exact arithmetic.
+ */
+
+#define CAT_(a, b) a##b
+#define CAT(a, b) CAT_(a, b)
+#define FN(name) CAT(name, SUFFIX)
+
+typedef struct {
+  REAL o[3], d[3];
+  REAL world_step, tmin, tmax;
+} FN(ray_t);
+
+static REAL FN(lerp)(REAL a, REAL b, REAL w) { return FMA(w, b - a, a); }
+
+static REAL FN(log_stop)(float stop) {
+  if (!(stop > 0.f)) return (REAL)(-INFINITY);
+  double L = log((double)stop);
+  REAL f = (REAL)L;
+  if ((double)f < L) f = NEXTAFTER(f, (REAL)INFINITY);
+  while ((double)NEXTAFTER(f, (REAL)(-INFINITY)) >= L) f = NEXTAFTER(f, (REAL)(-INFINITY));
+  return f;
+}
+
+/* calc_sh, svox2/csrc/include/render_util.cuh:332-363 (degree <= 2). */
+static void FN(calc_sh)(int bd, const REAL dir[3], REAL out[9]) {
+  const REAL C0 = (REAL)0.28209479177387814f, C1 = (REAL)0.4886025119029199f;
+  const REAL C20 = (REAL)1.0925484305920792f, C21 = (REAL)-1.0925484305920792f,
+             C22 = (REAL)0.31539156525252005f, C23 = (REAL)-1.0925484305920792f,
+             C24 = (REAL)0.5462742152960396f;
+  REAL x = dir[0], y = dir[1], z = dir[2];
+  out[0] = C0;
+  if (bd >= 4) {
+    out[1] = -C1 * y;
+    out[2] = C1 * z;
+    out[3] = -C1 * x;
+  }
+  if (bd >= 9) {
+    REAL xx = x * x, yy = y * y, zz = z * z, xy = x * y, yz = y * z, xz = x * z;
+    out[4] = C20 * xy;
+    out[5] = C21 * yz;
+    out[6] = (REAL)((double)C22 * (2.0 * (double)zz - (double)xx - (double)yy));
+    out[7] = C23 * xz;
+    out[8] = C24 * (xx - yy);
+  }
+}
+
+static REAL FN(rnorm3)(REAL x, REAL y, REAL z) {
+  double s = (double)x * (double)x + (double)y * (double)y + (double)z * (double)z;
+  return (REAL)(1.0 / sqrt(s));
+}
+
+static REAL FN(recip)(REAL d) { return (REAL)(1.0 / (double)d); }
+
+/* ConcentricSpheresIntersector, render_util.cuh:546-576. */
+static int FN(sphere_hit)(const REAL o[3], const REAL d[3], REAL r, REAL* out, int near) {
+  REAL dd = (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2];
+  REAL od = (o[0] * d[0] + o[1] * d[1]) + o[2] * d[2];
+  REAL oo = (o[0] * o[0] + o[1] * o[1]) + o[2] * o[2];
+  REAL q2a = 2 * dd, qb = 2 * od;
+  REAL f = qb * qb - (2 * q2a) * oo;
+  REAL det = f + ((2 * q2a) * r) * r;
+  if (det < 0) return 0;
+  REAL sq = SQRT(det);
+  *out = near ? (-qb - sq) / q2a : (-qb + sq) / q2a;
+  return 1;
+}
+
+/* ray_find_bounds, render_util.cuh:578-628 (+ transform_coord, _get_delta_scale). */
+static void FN(find_bounds)(FN(ray_t) * r, const REAL org[3], const REAL dir[3], const oracle_grid_t* g,
+                            const oracle_opt_t* opt) {
+  int i;
+  for (i = 0; i < 3; ++i) {
+    r->o[i] = FMA(org[i], (REAL)g->scaling[i], (REAL)g->offset[i]);
+    r->d[i] = dir[i] * (REAL)g->scaling[i];
+  }
+  REAL ds = FN(rnorm3)(r->d[0], r->d[1], r->d[2]);
+  for (i = 0; i < 3; ++i) r->d[i] = r->d[i] * ds;
+  r->world_step = ds * (REAL)opt->step;
+  if (opt->spheric) {
+    REAL so[3], sd[3];
+    for (i = 0; i < 3; ++i) {
+      REAL s = (REAL)2 / (REAL)g->size[i];
+      so[i] = FMA(r->o[i] + (REAL)0.5, s, (REAL)-1);
+      sd[i] = r->d[i] * s;
+    }
+    if (!FN(sphere_hit)(so, sd, (REAL)1, &r->tmax, 0) ||
+        !FN(sphere_hit)(so, sd, (REAL)1 - (REAL)opt->near_clip, &r->tmin, 1)) {
+      r->tmin = (REAL)1e-9f;
+      r->tmax = 0;
+    }
+  } else {
+    r->tmin = (REAL)opt->near_clip / r->world_step * (REAL)opt->step;
+    r->tmax = (REAL)2e3f;
+    for (i = 0; i < 3; ++i) {
+      REAL inv = FN(recip)(r->d[i]);
+      REAL t1 = ((REAL)-0.5 - r->o[i]) * inv;
+      REAL t2 = (((REAL)g->size[i] - (REAL)0.5) - r->o[i]) * inv;
+      if (r->d[i] != 0) {
+        r->tmin = FMAX(r->tmin, FMIN(t1, t2));
+        r->tmax = FMIN(r->tmax, FMAX(t1, t2));
+      }
+    }
+  }
+}
+
+/* compute_skip_dist, render_util.cuh:235-295 (pos_offset = 0). */
+static REAL FN(skip_dist)(int32_t link, const int l[3], const REAL pos[3], const REAL d[3]) {
+  uint32_t dist = (uint32_t)(-link), shift = dist - 1u;
+  uint32_t side = (uint32_t)((float)(1u << shift) - 1.f);
+  REAL tmin = 0, tmax = (REAL)1e9f;
+  int i;
+  for (i = 0; i < 3; ++i) {
+    int ul = ((l[i] >> shift) << shift) - l[i];
+    REAL inv = FN(recip)(d[i]);
+    REAL t1 = ((REAL)ul - pos[i]) * inv;
+    REAL t2 = ((REAL)((uint32_t)ul + side) - pos[i]) * inv;
+    if (d[i] != 0) {
+      tmin = FMAX(tmin, FMIN(t1, t2));
+      tmax = FMIN(tmax, FMAX(t1, t2));
+    }
+  }
+  return tmin > 0 ? 0 : tmax;
+}
+
+/* cam2world_ray + world2ndc, render_util.cuh:504-544.  c2w row-major, 4 columns. */
+static void FN(camera_ray)(int ix, int iy, const oracle_cam_t* cam, REAL dir[3], REAL org[3]) {
+  REAL x = (((REAL)ix + (REAL)0.5) - (REAL)cam->cx) / (REAL)cam->fx;
+  REAL y = (((REAL)iy + (REAL)0.5) - (REAL)cam->cy) / (REAL)cam->fy;
+  REAL z = SQRT((REAL)((double)(x * x + y * y) + 1.0));
+  int r, i;
+  x = x / z;
+  y = y / z;
+  z = (REAL)1 / z;
+  for (r = 0; r < 3; ++r) {
+    dir[r] = ((REAL)cam->c2w[4 * r] * x + (REAL)cam->c2w[4 * r + 1] * y) + (REAL)cam->c2w[4 * r + 2] * z;
+    org[r] = (REAL)cam->c2w[4 * r + 3];
+  }
+  if (cam->ndcx > 0.f) {
+    REAL t = ((REAL)1 - org[2]) / dir[2];
+    for (i = 0; i < 3; ++i) org[i] = FMA(t, dir[i], org[i]);
+    dir[0] = (REAL)cam->ndcx * (dir[0] / dir[2] - org[0] / org[2]);
+    dir[1] = (REAL)cam->ndcy * (dir[1] / dir[2] - org[1] / org[2]);
+    dir[2] = (REAL)2 / org[2];
+    org[0] = (REAL)cam->ndcx * (org[0] / org[2]);
+    org[1] = (REAL)cam->ndcy * (org[1] / org[2]);
+    org[2] = (REAL)1 - (REAL)2 / org[2];
+    REAL rn = FN(rnorm3)(dir[0], dir[1], dir[2]);
+    for (i = 0; i < 3; ++i) dir[i] = dir[i] * rn;
+  }
+}
+
+static void FN(atomic_add)(REAL* p, REAL v) {
+#pragma omp atomic
+  *p += v;
+}
+
+/* Per-sample state of the march, shared by the forward and backward loops. */
+typedef struct {
+  REAL pos[3];
+  int l[3];
+  const int32_t* lp;
+  int64_t base;
+} FN(sample_t);
+
+static void FN(locate)(const oracle_grid_t* g, const FN(ray_t) * r, REAL t, FN(sample_t) * s) {
+  const int64_t offy = g->size[2], offx = (int64_t)g->size[1] * g->size[2];
+  int j;
+  for (j = 0; j < 3; ++j) {
+    REAL p = FMA(t, r->d[j], r->o[j]);
+    p = FMIN(FMAX(p, (REAL)0), (REAL)g->size[j] - (REAL)1);
+    s->l[j] = (int)p;
+    if (s->l[j] > g->size[j] - 2) s->l[j] = g->size[j] - 2;
+    s->pos[j] = p - (REAL)s->l[j];
+  }
+  s->base = (int64_t)s->l[0] * offx + (int64_t)s->l[1] * offy + s->l[2];
+  s->lp = g->links + s->base;
+}
+
+/* trilerp_cuvol_one, render_util.cuh:71-91: z, then y, then x. */
+static REAL FN(trilerp)(const oracle_grid_t* g, const FN(sample_t) * s, const float* data, int stride, int idx) {
+  const int64_t offy = g->size[2], offx = (int64_t)g->size[1] * g->size[2];
+  const int64_t co[8] = {0, 1, offy, offy + 1, offx, offx + 1, offx + offy, offx + offy + 1};
+  REAL v[8];
+  int j;
+  for (j = 0; j < 8; ++j) {
+    int32_t lk = s->lp[co[j]];
+    v[j] = lk >= 0 ? (REAL)data[(int64_t)lk * stride + idx] : 0;
+  }
+  REAL ix0 = FN(lerp)(FN(lerp)(v[0], v[1], s->pos[2]), FN(lerp)(v[2], v[3], s->pos[2]), s->pos[1]);
+  REAL ix1 = FN(lerp)(FN(lerp)(v[4], v[5], s->pos[2]), FN(lerp)(v[6], v[7], s->pos[2]), s->pos[1]);
+  return FN(lerp)(ix0, ix1, s->pos[0]);
+}
+
+/* Colour sum per channel group, before the +0.5 offset. */
+static void FN(sample_colour)(const oracle_grid_t* g, const FN(sample_t) * s, const REAL basis[9], REAL col[3]) {
+  const int bd = g->basis_dim, C = 3 * bd;
+  int c;
+  col[0] = col[1] = col[2] = 0;
+  for (c = 0; c < C; ++c) col[c / bd] += FN(trilerp)(g, s, g->sh, C, c) * basis[c % bd];
+}
+
+/* trace_ray_cuvol, render_lerp_kernel_cuvol.cu:30-120.  Returns the colour and
+ * the log transmittance the reference reports (-1e3 after an early stop). */
+static void FN(fwd_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const REAL org[3], const REAL dir[3],
+                        REAL out[3], REAL* log_t, uint64_t* trace, uint64_t* n_eval) {
+  const REAL log_stop = FN(log_stop)(opt->stop_thresh), step = (REAL)opt->step;
+  REAL basis[9], outv[3] = {0, 0, 0}, t, lt = 0, ws;
+  FN(ray_t) r;
+  uint64_t h = 1469598103934665603ull;
+  int c;
+  FN(calc_sh)(g->basis_dim, dir, basis);
+  FN(find_bounds)(&r, org, dir, g, opt);
+  if (r.tmin > r.tmax) {
+    for (c = 0; c < 3; ++c) out[c] = (REAL)opt->bg;
+    *log_t = 0;
+    if (trace) *trace = h;
+    return;
+  }
+  t = r.tmin;
+  ws = r.world_step;
+  while (t <= r.tmax) {
+    FN(sample_t) s;
+    FN(locate)(g, &r, t, &s);
+    if (s.lp[0] < -1) {
+      REAL skip = FN(skip_dist)(s.lp[0], s.l, s.pos, r.d);
+      if (skip >= step) {
+        h = ((h ^ (uint64_t)s.base) * 1099511628211ull ^ 3ull) * 1099511628211ull;
+        t = t + CEIL(skip / step) * step;
+        continue;
+      }
+    }
+    REAL sigma = FN(trilerp)(g, &s, g->density, 1, 0);
+    if (opt->last_opaque && t + step > r.tmax) ws = (REAL)1e9f;
+    const int ev = sigma > (REAL)opt->sigma_thresh;
+    h = (h ^ (uint64_t)s.base) * 1099511628211ull;
+    h = (h ^ (ev ? 1ull : 2ull)) * 1099511628211ull;
+    if (ev) {
+      REAL col[3];
+      FN(sample_colour)(g, &s, basis, col);
+      const REAL pcnt = ws * sigma;
+      const REAL w = EXP(lt) * ((REAL)1 - EXP(-pcnt));
+      lt = lt - pcnt;
+      ++*n_eval;
+      for (c = 0; c < 3; ++c) outv[c] = outv[c] + w * FMAX(col[c] + (REAL)0.5, (REAL)0);
+      if (lt < log_stop) {
+        lt = (REAL)-1e3f;
+        break;
+      }
+    }
+    t = t + step;
+  }
+  for (c = 0; c < 3; ++c) out[c] = outv[c] + EXP(lt) * (REAL)opt->bg;
+  *log_t = lt;
+  if (trace) *trace = h;
+}
+
+/* trace_ray_cuvol_backward, render_lerp_kernel_cuvol.cu:227-383, forward order:
+ * accum starts at dot(colour, gout) and loses each sample's contribution. */
+static void FN(bwd_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const REAL org[3], const REAL dir[3],
+                        const REAL color[3], REAL log_t_in, const REAL gout[3], REAL beta_loss, REAL sparsity,
+                        REAL* grad_density, REAL* grad_sh, uint8_t* mask) {
+  const int bd = g->basis_dim, C = 3 * bd;
+  const int64_t offy = g->size[2], offx = (int64_t)g->size[1] * g->size[2];
+  const int64_t co[8] = {0, 1, offy, offy + 1, offx, offx + 1, offx + offy, offx + offy + 1};
+  const REAL log_stop = FN(log_stop)(opt->stop_thresh), step = (REAL)opt->step;
+  REAL basis[9], t, lt = 0, ws, accum;
+  FN(ray_t) r;
+  int c, j;
+  FN(calc_sh)(bd, dir, basis);
+  FN(find_bounds)(&r, org, dir, g, opt);
+  if (r.tmin > r.tmax) return;
+  accum = FMA(color[0], gout[0], FMA(color[1], gout[1], color[2] * gout[2]));
+  if (beta_loss > 0) {
+    const REAL tin = EXP(log_t_in);
+    beta_loss = (REAL)((double)beta_loss * (1.0 - (double)tin / ((double)((REAL)1 - tin) + 1e-3)));
+    accum += beta_loss;
+  }
+  t = r.tmin;
+  ws = r.world_step;
+  while (t <= r.tmax) {
+    FN(sample_t) s;
+    FN(locate)(g, &r, t, &s);
+    if (s.lp[0] < -1) {
+      REAL skip = FN(skip_dist)(s.lp[0], s.l, s.pos, r.d);
+      if (skip >= step) {
+        t = t + CEIL(skip / step) * step;
+        continue;
+      }
+    }
+    REAL sigma = FN(trilerp)(g, &s, g->density, 1, 0);
+    if (opt->last_opaque && t + step > r.tmax) ws = (REAL)1e9f;
+    if (sigma > (REAL)opt->sigma_thresh) {
+      REAL col[3], tot[3], in01[3], wts[8];
+      FN(sample_colour)(g, &s, basis, col);
+      const REAL pcnt = ws * sigma;
+      const REAL w = EXP(lt) * ((REAL)1 - EXP(-pcnt));
+      lt = lt - pcnt;
+      for (c = 0; c < 3; ++c) {
+        const REAL lc = col[c] + (REAL)0.5;
+        const REAL tc = FMAX(lc, (REAL)0);
+        in01[c] = (tc == lc) ? (REAL)1 : (REAL)0;
+        tot[c] = tc * gout[c];
+      }
+      const REAL tcs = (tot[0] + tot[2]) + tot[1];
+      accum = accum - w * tcs;
+      REAL gsig = ws * (tcs * EXP(lt) - accum);
+      if (sparsity > 0) gsig += sparsity * ((REAL)4 * sigma / ((REAL)1 + (REAL)2 * (sigma * sigma)));
+      /* trilerp_backward_cuvol_one(_density), render_util.cuh:94-153 */
+      {
+        const REAL ay = (REAL)1 - s.pos[1], az = (REAL)1 - s.pos[2];
+        REAL xo = (REAL)1 - s.pos[0];
+        wts[0] = ay * az * xo;
+        wts[1] = ay * s.pos[2] * xo;
+        wts[2] = s.pos[1] * az * xo;
+        wts[3] = s.pos[1] * s.pos[2] * xo;
+        xo = s.pos[0];
+        wts[4] = ay * az * xo;
+        wts[5] = ay * s.pos[2] * xo;
+        wts[6] = s.pos[1] * az * xo;
+        wts[7] = s.pos[1] * s.pos[2] * xo;
+      }
+      for (j = 0; j < 8; ++j) {
+        const int32_t lk = s.lp[co[j]];
+        if (lk < 0) continue;
+        if (grad_sh)
+          for (c = 0; c < C; ++c)
+            FN(atomic_add)(grad_sh + (int64_t)lk * C + c, wts[j] * (basis[c % bd] * (w * in01[c / bd] * gout[c / bd])));
+        if (grad_density) FN(atomic_add)(grad_density + lk, wts[j] * gsig);
+        if (mask) mask[lk] = 1;
+      }
+      if (lt < log_stop) break;
+    }
+    t = t + step;
+  }
+}
+
+/* Batch over rays: volume_render_cuvol / _fused / _backward
+ * (render_lerp_kernel_cuvol.cu:918-958, 1070-1152, 1010-1068).
+ *   mode 0: forward, rgb_out written.
+ *   mode 1: fused MSE: forward into rgb_out, gout = (rgb_out - rgb_gt) * 2/(3Q), backward.
+ *   mode 2: backward with grad_out; rgb_out must hold the forward colour (color_cache). */
+void FN(oracle_render)(const oracle_grid_t* g, const oracle_opt_t* opt, const float* origins, const float* dirs,
+                       int64_t Q, int mode, const float* rgb_gt, const float* grad_out, float beta_loss,
+                       float sparsity, REAL* rgb_out, REAL* grad_density, REAL* grad_sh, uint8_t* mask,
+                       uint64_t* trace, uint64_t* n_eval_total, int nthreads) {
+  int64_t q;
+  uint64_t total = 0;
+  const REAL norm = (REAL)2.f / (REAL)(float)(3 * Q);
+  if (nthreads < 1) nthreads = 1;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads) reduction(+ : total)
+  for (q = 0; q < Q; ++q) {
+    REAL org[3], dir[3], out[3], gout[3], lt = 0;
+    uint64_t ne = 0;
+    int i;
+    for (i = 0; i < 3; ++i) {
+      org[i] = (REAL)origins[q * 3 + i];
+      dir[i] = (REAL)dirs[q * 3 + i];
+    }
+    if (mode == 0 || mode == 1) {
+      FN(fwd_ray)(g, opt, org, dir, out, &lt, trace ? trace + q : NULL, &ne);
+      for (i = 0; i < 3; ++i) rgb_out[q * 3 + i] = out[i];
+    }
+    if (mode == 1) {
+      for (i = 0; i < 3; ++i) gout[i] = (out[i] - (REAL)rgb_gt[q * 3 + i]) * norm;
+      FN(bwd_ray)(g, opt, org, dir, out, lt, gout, (REAL)beta_loss / (REAL)Q, (REAL)sparsity, grad_density,
+                  grad_sh, mask);
+    } else if (mode == 2) {
+      for (i = 0; i < 3; ++i) {
+        out[i] = rgb_out[q * 3 + i];
+        gout[i] = (REAL)grad_out[q * 3 + i];
+      }
+      FN(bwd_ray)(g, opt, org, dir, out, 0, gout, 0, 0, grad_density, grad_sh, NULL);
+    }
+    total += ne;
+  }
+  if (n_eval_total) *n_eval_total += total;
+}
+
+/* volume_render_cuvol_image, render_lerp_kernel_cuvol.cu:960-1008 (+ kernel 650-690). */
+void FN(oracle_render_image)(const oracle_grid_t* g, const oracle_opt_t* opt, const oracle_cam_t* cam, REAL* out,
+                             uint64_t* trace, int nthreads) {
+  int64_t q, n = (int64_t)cam->width * cam->height;
+  if (nthreads < 1) nthreads = 1;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads)
+  for (q = 0; q < n; ++q) {
+    REAL org[3], dir[3], rgb[3], lt;
+    uint64_t ne = 0;
+    int i;
+    FN(camera_ray)((int)(q % cam->width), (int)(q / cam->width), cam, dir, org);
+    FN(fwd_ray)(g, opt, org, dir, rgb, &lt, trace ? trace + q : NULL, &ne);
+    for (i = 0; i < 3; ++i) out[q * 3 + i] = rgb[i];
+  }
+}
+
+/* sample_grid / sample_grid_backward, svox2/csrc/svox2_kernel.cu:10-176. */
+void FN(oracle_sample)(const oracle_grid_t* g, const float* pts, int64_t P, int want_colors, REAL* out_d,
+                       REAL* out_sh) {
+  const int C = 3 * g->basis_dim;
+  int64_t p;
+  for (p = 0; p < P; ++p) {
+    FN(sample_t) s;
+    int j, c;
+    const int64_t offy = g->size[2], offx = (int64_t)g->size[1] * g->size[2];
+    for (j = 0; j < 3; ++j) {
+      REAL v = FMA((REAL)pts[p * 3 + j], (REAL)g->scaling[j], (REAL)g->offset[j]);
+      v = FMIN(FMAX(v, (REAL)0), (REAL)g->size[j] - (REAL)1);
+      s.l[j] = (int)v;
+      if (s.l[j] > g->size[j] - 2) s.l[j] = g->size[j] - 2;
+      s.pos[j] = v - (REAL)s.l[j];
+    }
+    s.base = (int64_t)s.l[0] * offx + (int64_t)s.l[1] * offy + s.l[2];
+    s.lp = g->links + s.base;
+    out_d[p] = FN(trilerp)(g, &s, g->density, 1, 0);
+    if (want_colors)
+      for (c = 0; c < C; ++c) out_sh[p * C + c] = FN(trilerp)(g, &s, g->sh, C, c);
+  }
+}
+
+void FN(oracle_sample_backward)(const oracle_grid_t* g, const float* pts, int64_t P, int want_colors,
+                                const float* gd, const float* gsh, REAL* out_gd, REAL* out_gsh) {
+  const int C = 3 * g->basis_dim;
+  const int64_t offy = g->size[2], offx = (int64_t)g->size[1] * g->size[2];
+  const int64_t co[8] = {0, 1, offy, offy + 1, offx, offx + 1, offx + offy, offx + offy + 1};
+  int64_t p;
+  for (p = 0; p < P; ++p) {
+    REAL pos[3];
+    int l[3], j, c;
+    for (j = 0; j < 3; ++j) {
+      REAL v = FMA((REAL)pts[p * 3 + j], (REAL)g->scaling[j], (REAL)g->offset[j]);
+      v = FMIN(FMAX(v, (REAL)0), (REAL)g->size[j] - (REAL)1);
+      l[j] = (int)v;
+      if (l[j] > g->size[j] - 2) l[j] = g->size[j] - 2;
+      pos[j] = v - (REAL)l[j];
+    }
+    const int32_t* lp = g->links + (int64_t)l[0] * offx + (int64_t)l[1] * offy + l[2];
+    const REAL xb = pos[0], yb = pos[1], zb = pos[2];
+    const REAL xa = 1 - xb, ya = 1 - yb, za = 1 - zb;
+    for (j = 0; j < 8; ++j) {
+      const int32_t lk = lp[co[j]];
+      if (lk < 0) continue;
+      const REAL x = (j & 4) ? xb : xa, y = (j & 2) ? yb : ya, z = (j & 1) ? zb : za;
+      out_gd[lk] += (y * (x * (REAL)gd[p])) * z;
+      if (want_colors)
+        for (c = 0; c < C; ++c) out_gsh[(int64_t)lk * C + c] += (y * (x * (REAL)gsh[p * C + c])) * z;
+    }
+  }
+}
+
+/* tv_grad_sparse_kernel, svox2/csrc/loss_kernel.cu:178-246 (host 558-604), and
+ * tv_grad_kernel 111-176 (host 522-556) when cells == NULL. */
+void FN(oracle_tv_grad)(const int32_t* links, const int size[3], const float* data, int64_t n_rows, int ncols,
+                        const int32_t* cells, int64_t n_cells, int start, int end, float scale, int ignore_edge,
+                        int ignore_last_z, REAL* grad, uint8_t* mask) {
+  const int X = size[0], Y = size[1], Z = size[2];
+  const int64_t offy = Z, offx = (int64_t)Y * Z;
+  const REAL sx = (REAL)(X * (1.f / 256.f)), sy = (REAL)(Y * (1.f / 256.f)), sz = (REAL)(Z * (1.f / 256.f));
+  const int dense = cells == NULL;
+  const int64_t ncell = dense ? (int64_t)(X - 1) * (Y - 1) * (Z - 1) : n_cells;
+  const REAL sc = (REAL)(scale / (float)(int)ncell);
+  int64_t k;
+  int idx;
+  (void)n_rows;
+  for (k = 0; k < ncell; ++k) {
+    int x, y, z;
+    if (dense) {
+      z = (int)(k % (Z - 1));
+      y = (int)((k / (Z - 1)) % (Y - 1));
+      x = (int)(k / ((int64_t)(Z - 1) * (Y - 1)));
+    } else {
+      int xyz = cells[k];
+      z = xyz % Z;
+      y = (xyz / Z) % Y;
+      x = (xyz / Z) / Y;
+    }
+    const int32_t* lp = links + x * offx + y * offy + z;
+    const int32_t l000 = lp[0];
+    if (ignore_edge && l000 == 0) continue;
+    int32_t l001, l010, l100;
+    if (dense) {
+      l001 = lp[1];
+      l010 = lp[offy];
+      l100 = lp[offx];
+    } else {
+      l001 = (z + 1 < Z && (!ignore_last_z || z != Z - 2)) ? lp[1] : 0;
+      l010 = y + 1 < Y ? lp[offy] : 0;
+      l100 = x + 1 < X ? lp[offx] : 0;
+      if (ignore_last_z && z == Z - 2) continue;
+    }
+    for (idx = start; idx < end; ++idx) {
+      const REAL v000 = l000 >= 0 ? (REAL)data[(int64_t)l000 * ncols + idx] : 0;
+      const REAL nul = ignore_edge ? v000 : 0;
+      const REAL v001 = l001 >= 0 ? (REAL)data[(int64_t)l001 * ncols + idx] : nul;
+      const REAL v010 = l010 >= 0 ? (REAL)data[(int64_t)l010 * ncols + idx] : nul;
+      const REAL v100 = l100 >= 0 ? (REAL)data[(int64_t)l100 * ncols + idx] : nul;
+      REAL dx = v100 - v000, dy = v010 - v000, dz = v001 - v000;
+      const REAL idelta = sc / SQRT((REAL)1e-9f + dx * dx + dy * dy + dz * dz);
+      dx = dx * sx;
+      dy = dy * sy;
+      dz = dz * sz;
+      const REAL sm = -((dx + dy) + dz);
+      if (dense) {
+        if (dx != 0 && l100 >= 0) grad[(int64_t)l100 * ncols + idx] += dx * idelta;
+        if (dy != 0 && l010 >= 0) grad[(int64_t)l010 * ncols + idx] += dy * idelta;
+        if (dz != 0 && l001 >= 0) grad[(int64_t)l001 * ncols + idx] += dz * idelta;
+        if (l000 >= 0) grad[(int64_t)l000 * ncols + idx] += sm * idelta;
+      } else {
+        const int32_t lks[4] = {l000, l001, l010, l100};
+        const REAL vals[4] = {sm, dz, dy, dx};
+        int q;
+        for (q = 0; q < 4; ++q)
+          if (lks[q] >= 0 && vals[q] != 0) {
+            grad[(int64_t)lks[q] * ncols + idx] += vals[q] * idelta;
+            if (mask) mask[lks[q]] = 1;
+          }
+      }
+    }
+  }
+}
+
+/* rmsprop_once / sgd_once, svox2/csrc/optim_kernel.cu:15-25, 97-103, over the
+ * rows selected by kind (0 all, 1 none, 2 mask, 3 index list). */
+void FN(oracle_optim)(int rmsprop, REAL* data, REAL* rms, REAL* grad, int64_t n_rows, int ncols, int kind,
+                      const uint8_t* mask, const int64_t* index, int64_t n_index, float beta, float lr, float eps,
+                      float minval, float lr_last) {
+  int64_t k, nr = kind == 3 ? n_index : n_rows;
+  int c;
+  if (kind == 1) return;
+  if (lr_last < 0.f) lr_last = lr;
+  for (k = 0; k < nr; ++k) {
+    const int64_t row = kind == 3 ? index[k] : k;
+    if (kind == 2 && !mask[row]) continue;
+    for (c = 0; c < ncols; ++c) {
+      const int64_t off = row * ncols + c;
+      const REAL l = (REAL)(c == ncols - 1 ? lr_last : lr);
+      const REAL g = grad[off];
+      if (rmsprop) {
+        const REAL g2 = g * g;
+        REAL r = rms[off];
+        r = (r == 0) ? g2 : FMA((REAL)beta, r - g2, g2);
+        rms[off] = r;
+        data[off] = FMAX(data[off] - (l * g) / (SQRT(r) + (REAL)eps), (REAL)minval);
+      } else {
+        data[off] = data[off] - l * g;
+      }
+      grad[off] = 0;
+    }
+  }
+}
+
+#undef FN
+#undef CAT
+#undef CAT_

@@ -1,0 +1,211 @@
+// Total-variation gradients on the voxel grid.
+//
+// Replaces svox2/csrc/loss_kernel.cu: tv_grad_kernel 111-176 (dense over all
+// cells) and tv_grad_sparse_kernel 178-246 (a list of cells, the training
+// default), with their host launchers 522-604.  One thread per (cell, channel),
+// channels innermost so that a warp reads consecutive coefficients of the same
+// voxel rows.  The reference's edge conventions are kept exactly:
+//   * sparse: a neighbour outside the grid reads link 0 (voxel 0), not -1;
+//   * ignore_edge && link(cell) == 0 skips the cell;
+//   * ignore_last_z skips cells with z == size2 - 2 (and reads no +z neighbour there);
+//   * the finite differences are normalised with rsqrt of the UNSCALED squared
+//     gradient, then scaled by size/256 per axis; scale is divided by the
+//     number of cells.
+#include "common.cuh"
+
+namespace svx {
+namespace {
+
+struct TvArgs {
+  const int32_t* links;
+  int X, Y, Z;
+  const void* data;
+  long long ncols;
+  int start, nch;
+  float scale;  // already divided by the number of cells
+  int ignore_edge, ignore_last_z;
+  float* grad;
+  uint8_t* mask;
+};
+
+template <typename T>
+__device__ __forceinline__ float rd(const TvArgs& a, int lnk, int idx) {
+  return to_f32<T>(reinterpret_cast<const T*>(a.data)[(long long)lnk * a.ncols + idx]);
+}
+
+__device__ __forceinline__ float inv_norm(float dx, float dy, float dz, float scale) {
+  return __fmul_rn(scale, rsqrtf(fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, 1e-9f)))));
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) tv_sparse_kernel(TvArgs a, const int32_t* __restrict__ cells,
+                                                        long long n) {
+  const long long total = n * a.nch;
+  const float sx = a.X * (1.f / 256.f), sy = a.Y * (1.f / 256.f), sz = a.Z * (1.f / 256.f);
+  for (long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x; tid < total;
+       tid += (long long)gridDim.x * blockDim.x) {
+    const int idx = (int)(tid % a.nch) + a.start;
+    const int xyz = __ldg(cells + tid / a.nch);
+    const int z = xyz % a.Z, xy = xyz / a.Z;
+    const int y = xy % a.Y, x = xy / a.Y;
+    const long long offy = a.Z, offx = (long long)a.Y * a.Z;
+    const int32_t* lp = a.links + x * offx + y * offy + z;
+    const int l000 = __ldg(lp);
+    if (a.ignore_edge && l000 == 0) continue;
+    const int l001 = (z + 1 < a.Z && (!a.ignore_last_z || z != a.Z - 2)) ? __ldg(lp + 1) : 0;
+    const int l010 = (y + 1 < a.Y) ? __ldg(lp + offy) : 0;
+    const int l100 = (x + 1 < a.X) ? __ldg(lp + offx) : 0;
+    if (a.ignore_last_z && z == a.Z - 2) continue;
+    const float v000 = l000 >= 0 ? rd<T>(a, l000, idx) : 0.f;
+    const float nul = a.ignore_edge ? v000 : 0.f;
+    const float v001 = l001 >= 0 ? rd<T>(a, l001, idx) : nul;
+    const float v010 = l010 >= 0 ? rd<T>(a, l010, idx) : nul;
+    const float v100 = l100 >= 0 ? rd<T>(a, l100, idx) : nul;
+    float dx = __fsub_rn(v100, v000), dy = __fsub_rn(v010, v000), dz = __fsub_rn(v001, v000);
+    const float idelta = inv_norm(dx, dy, dz, a.scale);
+    dx = __fmul_rn(dx, sx);
+    dy = __fmul_rn(dy, sy);
+    dz = __fmul_rn(dz, sz);
+    const float sm = -__fadd_rn(__fadd_rn(dx, dy), dz);
+    auto add = [&](int lnk, float v) {
+      if (lnk >= 0 && v != 0.f) {
+        atomicAdd(a.grad + (long long)lnk * a.ncols + idx, __fmul_rn(v, idelta));
+        if (a.mask != nullptr) a.mask[lnk] = 1;
+      }
+    };
+    add(l000, sm);
+    add(l001, dz);
+    add(l010, dy);
+    add(l100, dx);
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) tv_dense_kernel(TvArgs a) {
+  const long long ncell = (long long)(a.X - 1) * (a.Y - 1) * (a.Z - 1);
+  const long long total = ncell * a.nch;
+  const float sx = a.X * (1.f / 256.f), sy = a.Y * (1.f / 256.f), sz = a.Z * (1.f / 256.f);
+  for (long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x; tid < total;
+       tid += (long long)gridDim.x * blockDim.x) {
+    const int idx = (int)(tid % a.nch) + a.start;
+    const long long xyz = tid / a.nch;
+    const int z = (int)(xyz % (a.Z - 1));
+    const long long xy = xyz / (a.Z - 1);
+    const int y = (int)(xy % (a.Y - 1)), x = (int)(xy / (a.Y - 1));
+    const long long offy = a.Z, offx = (long long)a.Y * a.Z;
+    const int32_t* lp = a.links + x * offx + y * offy + z;
+    const int l000 = __ldg(lp);
+    if (a.ignore_edge && l000 == 0) continue;
+    const int l100 = __ldg(lp + offx), l010 = __ldg(lp + offy), l001 = __ldg(lp + 1);
+    const float v000 = l000 >= 0 ? rd<T>(a, l000, idx) : 0.f;
+    const float v100 = l100 >= 0 ? rd<T>(a, l100, idx) : (a.ignore_edge ? v000 : 0.f);
+    const float v010 = l010 >= 0 ? rd<T>(a, l010, idx) : (a.ignore_edge ? v000 : 0.f);
+    const float v001 = l001 >= 0 ? rd<T>(a, l001, idx) : (a.ignore_edge ? v000 : 0.f);
+    float dx = __fsub_rn(v100, v000), dy = __fsub_rn(v010, v000), dz = __fsub_rn(v001, v000);
+    const float idelta = inv_norm(dx, dy, dz, a.scale);
+    dx = __fmul_rn(dx, sx);
+    dy = __fmul_rn(dy, sy);
+    dz = __fmul_rn(dz, sz);
+    float* g = a.grad;
+    if (dx != 0.f && l100 >= 0) atomicAdd(g + (long long)l100 * a.ncols + idx, __fmul_rn(dx, idelta));
+    if (dy != 0.f && l010 >= 0) atomicAdd(g + (long long)l010 * a.ncols + idx, __fmul_rn(dy, idelta));
+    if (dz != 0.f && l001 >= 0) atomicAdd(g + (long long)l001 * a.ncols + idx, __fmul_rn(dz, idelta));
+    if (l000 >= 0)
+      atomicAdd(g + (long long)l000 * a.ncols + idx,
+                __fmul_rn(-__fadd_rn(__fadd_rn(dx, dy), dz), idelta));
+  }
+}
+
+int make_tv(const int32_t* links, const int32_t size[3], const svx_table_t* data, int start, int end,
+            float* grad, TvArgs* a) {
+  SVX_REQUIRE(links && size && data && data->data && grad, SVX_ERR_INVALID, "null argument");
+  for (int i = 0; i < 3; ++i)
+    SVX_REQUIRE(size[i] >= 2, SVX_ERR_INVALID, "links size[%d] = %d must be >= 2", i, size[i]);
+  SVX_REQUIRE(data->n_cols >= 1, SVX_ERR_INVALID, "data has %d columns", data->n_cols);
+  SVX_REQUIRE(0 <= start && start < end && end <= data->n_cols, SVX_ERR_INVALID,
+              "channel range [%d, %d) outside [0, %d)", start, end, data->n_cols);
+  SVX_REQUIRE(data->dtype == SVX_F32 || data->dtype == SVX_BF16 || data->dtype == SVX_F16, SVX_ERR_INVALID,
+              "data dtype %d unknown", data->dtype);
+  a->links = links;
+  a->X = size[0];
+  a->Y = size[1];
+  a->Z = size[2];
+  a->data = data->data;
+  a->ncols = data->n_cols;
+  a->start = start;
+  a->nch = end - start;
+  a->grad = grad;
+  a->mask = nullptr;
+  return SVX_OK;
+}
+
+unsigned grid_for(long long total) {
+  long long b = (total + 255) / 256;
+  const long long cap = (long long)num_sms() * 32;
+  if (b > cap) b = cap;
+  return (unsigned)(b < 1 ? 1 : b);
+}
+
+}  // namespace
+}  // namespace svx
+
+using namespace svx;
+
+extern "C" int svx_tv_grad(const int32_t* links, const int32_t size[3], const svx_table_t* data,
+                           int32_t start_dim, int32_t end_dim, float scale, int32_t use_logalpha,
+                           float logalpha_delta, int32_t ignore_edge, float ndc_coeffx, float ndc_coeffy,
+                           float* grad, void* stream) {
+  (void)use_logalpha;
+  (void)logalpha_delta;
+  (void)ndc_coeffx;
+  (void)ndc_coeffy;
+  clear_error();
+  TvArgs a;
+  int rc = make_tv(links, size, data, start_dim, end_dim, grad, &a);
+  if (rc) return rc;
+  const long long ncell = (long long)(a.X - 1) * (a.Y - 1) * (a.Z - 1);
+  // the reference divides by the cell count held in an int (loss_kernel.cu:539)
+  a.scale = scale / (float)(int)ncell;
+  a.ignore_edge = ignore_edge != 0;
+  a.ignore_last_z = 0;
+  cudaStream_t st = as_stream(stream);
+  const unsigned blocks = grid_for(ncell * a.nch);
+  switch (data->dtype) {
+    case SVX_F32: tv_dense_kernel<float><<<blocks, 256, 0, st>>>(a); break;
+    case SVX_BF16: tv_dense_kernel<__nv_bfloat16><<<blocks, 256, 0, st>>>(a); break;
+    default: tv_dense_kernel<__half><<<blocks, 256, 0, st>>>(a);
+  }
+  SVX_LAUNCH_CHECK("tv_dense_kernel");
+  return SVX_OK;
+}
+
+extern "C" int svx_tv_grad_sparse(const int32_t* links, const int32_t size[3], const svx_table_t* data,
+                                  const int32_t* rand_cells, int64_t n_cells, uint8_t* mask_out,
+                                  int32_t start_dim, int32_t end_dim, float scale, int32_t use_logalpha,
+                                  float logalpha_delta, int32_t ignore_edge, int32_t ignore_last_z,
+                                  float ndc_coeffx, float ndc_coeffy, float* grad, void* stream) {
+  (void)use_logalpha;
+  (void)logalpha_delta;
+  (void)ndc_coeffx;
+  (void)ndc_coeffy;
+  clear_error();
+  TvArgs a;
+  int rc = make_tv(links, size, data, start_dim, end_dim, grad, &a);
+  if (rc) return rc;
+  SVX_REQUIRE(n_cells >= 0, SVX_ERR_INVALID, "n_cells < 0");
+  if (n_cells == 0) return SVX_OK;
+  SVX_REQUIRE(rand_cells != nullptr, SVX_ERR_INVALID, "rand_cells is null");
+  a.scale = scale / (float)(int)n_cells;
+  a.ignore_edge = ignore_edge != 0;
+  a.ignore_last_z = ignore_last_z != 0;
+  a.mask = mask_out;
+  cudaStream_t st = as_stream(stream);
+  const unsigned blocks = grid_for(n_cells * a.nch);
+  switch (data->dtype) {
+    case SVX_F32: tv_sparse_kernel<float><<<blocks, 256, 0, st>>>(a, rand_cells, n_cells); break;
+    case SVX_BF16: tv_sparse_kernel<__nv_bfloat16><<<blocks, 256, 0, st>>>(a, rand_cells, n_cells); break;
+    default: tv_sparse_kernel<__half><<<blocks, 256, 0, st>>>(a, rand_cells, n_cells);
+  }
+  SVX_LAUNCH_CHECK("tv_sparse_kernel");
+  return SVX_OK;
+}

@@ -1,0 +1,112 @@
+"""Generate golden vectors from the REFERENCE implementation (sxyu/svox2's own
+pure-PyTorch CPU path) for the oracle's pinning tests.
+
+Run in a container where the reference source tree is available:
+    python tests/golden/make_golden.py /path/to/reference
+It imports the reference package read-only, builds small seeded grids, and
+records inputs and outputs of
+  * SparseGrid.volume_render(use_kernel=False) + autograd of F.mse_loss
+    (svox2/svox2.py:658-884, the reference's gradcheck path), and
+  * SparseGrid.sample(use_kernel=False) + autograd (svox2/svox2.py:576-653),
+into tests/golden/*.npz.  sigma_thresh = stop_thresh = 0 so that the CPU
+path's semantics coincide with the CUDA kernel's (the reference's own
+test/test_render_gradcheck.py uses the same setting).
+"""
+from __future__ import annotations
+
+import sys
+import warnings
+from pathlib import Path
+
+import numpy as np
+import torch
+import torch.nn.functional as F
+
+OUT = Path(__file__).resolve().parent
+
+
+def _rays(n, gen):
+    o = torch.randn((n, 3), generator=gen)
+    o = 1.5 * o / o.norm(dim=-1, keepdim=True)
+    tgt = torch.rand((n, 3), generator=gen) - 0.5
+    d = tgt - o
+    d = d / d.norm(dim=-1, keepdim=True)
+    gt = torch.rand((n, 3), generator=gen)
+    return o, d, gt
+
+
+def render_case(svox2, name, reso, basis_dim, occupancy, z_order, n_rays, bg, step, seed):
+    gen = torch.Generator().manual_seed(seed)
+    grid = svox2.SparseGrid(reso=reso, basis_dim=basis_dim, use_z_order=z_order, device="cpu")
+    links = grid.links.clone()
+    if occupancy is not None:
+        # drop voxels outside a random ball union, re-index rows in raster order
+        n3 = links.numel()
+        keep = torch.rand(links.shape, generator=gen) < occupancy
+        new = torch.full(links.shape, -1, dtype=torch.int32)
+        new[keep] = torch.arange(int(keep.sum()), dtype=torch.int32)
+        links = new
+        grid.links = links
+        N = int(keep.sum())
+        grid.density_data = torch.nn.Parameter(torch.zeros(N, 1))
+        grid.sh_data = torch.nn.Parameter(torch.zeros(N, 3 * basis_dim))
+    N = grid.density_data.shape[0]
+    dens = torch.clamp(torch.randn((N, 1), generator=gen) * 3.0 + 2.0, min=0.0)
+    sh = torch.randn((N, 3 * basis_dim), generator=gen) * 0.3
+    grid.density_data.data[:] = dens
+    grid.sh_data.data[:] = sh
+    grid.opt.sigma_thresh = 0.0
+    grid.opt.stop_thresh = 0.0
+    grid.opt.background_brightness = bg
+    grid.opt.step_size = step
+    o, d, gt = _rays(n_rays, gen)
+    rgb = grid.volume_render(svox2.Rays(o, d), use_kernel=False)
+    loss = F.mse_loss(rgb, gt)
+    loss.backward()
+    gsz = grid._grid_size()
+    np.savez_compressed(
+        OUT / f"render_{name}.npz",
+        links=links.numpy().astype(np.int32), density=dens.numpy(), sh=sh.numpy(),
+        basis_dim=basis_dim, offset=(grid._offset * gsz - 0.5).numpy(), scaling=(grid._scaling * gsz).numpy(),
+        origins=o.numpy(), dirs=d.numpy(), rgb_gt=gt.numpy(), bg=bg, step=step,
+        rgb=rgb.detach().numpy(), grad_density=grid.density_data.grad.numpy(),
+        grad_sh=grid.sh_data.grad.numpy())
+    print(name, "rays", n_rays, "voxels", N, "rgb mean", float(rgb.mean()))
+
+
+def sample_case(svox2, name, reso, basis_dim, n_points, seed):
+    gen = torch.Generator().manual_seed(seed)
+    grid = svox2.SparseGrid(reso=reso, basis_dim=basis_dim, device="cpu")
+    N = grid.density_data.shape[0]
+    grid.density_data.data[:] = torch.randn((N, 1), generator=gen)
+    grid.sh_data.data[:] = torch.randn((N, 3 * basis_dim), generator=gen)
+    pts = torch.rand((n_points, 3), generator=gen) * 2.4 - 1.2   # includes points outside the grid
+    gd_out = torch.randn((n_points, 1), generator=gen)
+    gs_out = torch.randn((n_points, 3 * basis_dim), generator=gen)
+    d, s = grid.sample(pts.clone(), use_kernel=False)
+    (d * gd_out).sum().add_((s * gs_out).sum()).backward()
+    gsz = grid._grid_size()
+    np.savez_compressed(
+        OUT / f"sample_{name}.npz",
+        links=grid.links.numpy().astype(np.int32), density=grid.density_data.data.numpy(),
+        sh=grid.sh_data.data.numpy(), basis_dim=basis_dim, offset=(grid._offset * gsz - 0.5).numpy(),
+        scaling=(grid._scaling * gsz).numpy(), points=pts.numpy(), grad_out_density=gd_out.numpy(),
+        grad_out_sh=gs_out.numpy(), out_density=d.detach().numpy(), out_sh=s.detach().numpy(),
+        grad_density=grid.density_data.grad.numpy(), grad_sh=grid.sh_data.grad.numpy())
+    print(name, "points", n_points)
+
+
+def main(ref_root: str):
+    sys.path.insert(0, ref_root)
+    warnings.filterwarnings("ignore")
+    import svox2  # the reference package (CPU path; its CUDA extension is not needed)
+    torch.set_num_threads(4)
+    render_case(svox2, "dense12_sh9", 12, 9, None, False, 48, 1.0, 0.5, 11)
+    render_case(svox2, "sparse16_sh9", 16, 9, 0.35, False, 48, 1.0, 0.5, 12)
+    render_case(svox2, "morton16_sh4", 16, 4, None, True, 40, 0.25, 0.7, 13)
+    render_case(svox2, "dense10x12x14_sh1", (10, 12, 14), 1, None, False, 40, 0.0, 0.5, 14)
+    sample_case(svox2, "dense10_sh9", 10, 9, 300, 15)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

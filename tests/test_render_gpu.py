@@ -1,0 +1,229 @@
+"""Parity of the CUDA ray march / fused adjoint / backward / image render with
+the CPU oracle, through the reference-facing operator API (svox2_gb300.csrc ->
+C ABI).  Every case checks:
+  * sample indexing bit for bit (per-ray hash of every sample's cell and
+    evaluated flag, plus skips) and the evaluated-sample count;
+  * colours within 1e-5 relative of the float32 oracle;
+  * gradients within 1e-4 relative + 1e-5 of the largest entry (atomic order);
+  * the touched-voxel mask exactly;
+and prints the error of the kernel and of the float32 oracle against the
+float64 oracle."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+from svox2_gb300 import synthetic as S
+
+from helpers import assert_grad, assert_rgb, grid_pair, opt_struct, rays_pair, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _stats(Q):
+    return {"eval_samples": torch.zeros(1, dtype=torch.int64, device="cuda"),
+            "ray_trace": torch.zeros(Q, dtype=torch.int64, device="cuda")}
+
+
+def _run_fused(spec, og, rays, o, d, gt, opt, oopt, beta=0.0, sparsity=0.0, check_f64=True):
+    from svox2_gb300 import csrc as C
+    Q = o.shape[0]
+    N = og.density.shape[0]
+    rgb = torch.zeros((Q, 3), device="cuda")
+    grads = C.GridOutputGrads()
+    grads.grad_density_out = torch.zeros((N, 1), device="cuda")
+    grads.grad_sh_out = torch.zeros((N, og.sh.shape[1]), device="cuda")
+    grads.mask_out = torch.zeros((N,), dtype=torch.bool, device="cuda")
+    st = _stats(Q)
+    C.volume_render_cuvol_fused(spec, rays, opt, gt.cuda(), beta, sparsity, rgb, grads, stats=st)
+    torch.cuda.synchronize()
+    ref = O.render(og, oopt, o.numpy(), d.numpy(), mode=1, rgb_gt=gt.numpy(), beta_loss=beta,
+                   sparsity_loss=sparsity, prec="f32", trace=True)
+    k_trace = st["ray_trace"].cpu().numpy().view(np.uint64)
+    mism = int((k_trace != ref["trace"]).sum())
+    assert mism == 0, f"sample indexing differs on {mism} of {Q} rays"
+    assert int(st["eval_samples"].item()) == ref["n_eval"]
+    assert_rgb(rgb.cpu().numpy(), ref["rgb"], "rgb")
+    assert_grad(grads.grad_density_out.cpu().numpy(), ref["grad_density"], "grad_density")
+    assert_grad(grads.grad_sh_out.cpu().numpy(), ref["grad_sh"], "grad_sh")
+    np.testing.assert_array_equal(grads.mask_out.cpu().numpy(), ref["mask"])
+    if check_f64:
+        r64 = O.render(og, oopt, o.numpy(), d.numpy(), mode=1, rgb_gt=gt.numpy(), beta_loss=beta,
+                       sparsity_loss=sparsity, prec="f64")
+        print(f"vs f64: kernel rgb {rel_err(rgb.cpu().numpy(), r64['rgb']):.2e} "
+              f"gsh {rel_err(grads.grad_sh_out.cpu().numpy(), r64['grad_sh']):.2e} "
+              f"gd {rel_err(grads.grad_density_out.cpu().numpy(), r64['grad_density']):.2e} | "
+              f"oracle32 rgb {rel_err(ref['rgb'], r64['rgb']):.2e} gsh {rel_err(ref['grad_sh'], r64['grad_sh']):.2e} "
+              f"gd {rel_err(ref['grad_density'], r64['grad_density']):.2e}; n_eval {ref['n_eval']}")
+    return rgb, grads, ref
+
+
+CASES = {
+    # name: (reso, occupancy, basis_dim, sh dtype, n rays, options)
+    "dense32_sh9": (32, None, 9, torch.float32, 1024, {}),
+    "sparse48_sh9": (48, 0.2, 9, torch.float32, 1024, {}),
+    "noncubic_sh4": ((20, 28, 36), 0.3, 4, torch.float32, 768, {"bg": 0.3}),
+    "dense24_sh1": (24, None, 1, torch.float32, 512, {"bg": 0.0}),
+    "sparse40_bf16": (40, 0.25, 9, torch.bfloat16, 768, {}),
+    "sparse40_f16": (40, 0.25, 9, torch.float16, 768, {}),
+    "step03_no_stop": (24, None, 9, torch.float32, 512, {"step": 0.3, "stop_thresh": 0.0}),
+    "thresh_hi": (32, 0.4, 9, torch.float32, 768, {"sigma_thresh": 5.0, "stop_thresh": 1e-3}),
+    "near_clip": (32, None, 9, torch.float32, 512, {"near_clip": 0.4}),
+    "spheric_clip": (32, None, 9, torch.float32, 512, {"spheric": True, "near_clip": 0.1}),
+    "last_opaque": (32, 0.5, 9, torch.float32, 512, {"last_opaque": True}),
+}
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_fused_parity(name):
+    reso, occ, bd, dt, Q, kw = CASES[name]
+    g = S.make_grid(reso, occupancy=occ, basis_dim=9, seed=3)
+    spec, og = grid_pair(g, basis_dim=bd, sh_dtype=dt)
+    o, d, gt = S.make_rays(Q, seed=4)
+    opt, oopt = opt_struct(**kw)
+    _run_fused(spec, og, rays_pair(o, d), o, d, gt, opt, oopt)
+
+
+def test_fused_beta_sparsity():
+    g = S.make_grid(32, occupancy=0.3, seed=5)
+    spec, og = grid_pair(g)
+    o, d, gt = S.make_rays(768, seed=6)
+    opt, oopt = opt_struct()
+    _run_fused(spec, og, rays_pair(o, d), o, d, gt, opt, oopt, beta=0.5, sparsity=0.01)
+
+
+def test_long_rays_colour_cache_and_checkpoint_thinning():
+    """Rays with > 192 evaluated samples (colours re-gathered in the reverse pass)
+    and > 64 evaluated segments (checkpoints thinned to every 2nd and 4th segment)."""
+    reso = (3, 3, 1800)
+    g = S.make_grid(reso, seed=7, density_mode="normal53")
+    g.density.mul_(0.004)   # transparent enough that rays run the whole length
+    spec, og = grid_pair(g)
+    Q = 96
+    gen = torch.Generator().manual_seed(8)
+    o = torch.zeros((Q, 3))
+    o[:, 0] = (torch.rand(Q, generator=gen) - 0.5) * 1.0
+    o[:, 1] = (torch.rand(Q, generator=gen) - 0.5) * 1.0
+    o[:, 2] = -1.3
+    d = torch.zeros((Q, 3))
+    d[:, 0] = (torch.rand(Q, generator=gen) - 0.5) * 1e-3
+    d[:, 1] = (torch.rand(Q, generator=gen) - 0.5) * 1e-3
+    d[:, 2] = 1.0
+    d = d / d.norm(dim=-1, keepdim=True)
+    gt = torch.rand((Q, 3), generator=gen)
+    opt, oopt = opt_struct(stop_thresh=0.0)
+    _, _, ref = _run_fused(spec, og, rays_pair(o, d), o, d, gt, opt, oopt)
+    assert ref["n_eval"] > Q * 2500
+
+
+def test_edge_cases():
+    from svox2_gb300 import csrc as C
+    # all-empty grid: every ray renders the background, no gradient, no mask
+    g = S.make_grid(16, seed=9)
+    g.links.fill_(-1)
+    spec, og = grid_pair(g)
+    o, d, gt = S.make_rays(256, seed=10)
+    opt, oopt = opt_struct(bg=0.7)
+    rgb, grads, _ = _run_fused(spec, og, rays_pair(o, d), o, d, gt, opt, oopt)
+    assert torch.allclose(rgb, torch.full_like(rgb, 0.7))
+    assert not grads.mask_out.any()
+    # smallest grid (2^3), axis-aligned rays (zero direction components), rays that miss
+    g = S.make_grid(2, seed=11)
+    spec, og = grid_pair(g)
+    o = torch.tensor([[0.0, 0.0, -3.0], [0.1, -2.5, 0.2], [5.0, 5.0, 5.0], [0.3, 0.2, -2.0], [-2.0, 0.5, 0.5]])
+    d = torch.tensor([[0.0, 0.0, 1.0], [0.0, 1.0, 0.0], [1.0, 0.0, 0.0], [0.0, 0.6, 0.8], [1.0, 0.0, 0.0]])
+    gt = torch.rand((5, 3), generator=torch.Generator().manual_seed(0))
+    opt, oopt = opt_struct()
+    _run_fused(spec, og, rays_pair(o, d), o, d, gt, opt, oopt)
+    # zero rays: no launch, no error
+    r = C.RaysSpec()
+    r.origins = torch.zeros((0, 3), device="cuda")
+    r.dirs = torch.zeros((0, 3), device="cuda")
+    out = C.volume_render_cuvol(spec, r, opt)
+    assert out.shape == (0, 3)
+
+
+def test_forward_and_backward_only():
+    from svox2_gb300 import csrc as C
+    g = S.make_grid(40, occupancy=0.3, seed=12)
+    spec, og = grid_pair(g)
+    o, d, gt = S.make_rays(1024, seed=13)
+    rays = rays_pair(o, d)
+    opt, oopt = opt_struct()
+    st = _stats(1024)
+    rgb = C.volume_render_cuvol(spec, rays, opt, stats=st)
+    torch.cuda.synchronize()
+    ref = O.render(og, oopt, o.numpy(), d.numpy(), mode=0, trace=True)
+    assert (st["ray_trace"].cpu().numpy().view(np.uint64) == ref["trace"]).all()
+    assert_rgb(rgb.cpu().numpy(), ref["rgb"], "forward")
+    # backward with an arbitrary upstream gradient
+    go = torch.randn((1024, 3), generator=torch.Generator().manual_seed(14))
+    N = og.density.shape[0]
+    grads = C.GridOutputGrads()
+    grads.grad_density_out = torch.zeros((N, 1), device="cuda")
+    grads.grad_sh_out = torch.zeros((N, 27), device="cuda")
+    C.volume_render_cuvol_backward(spec, rays, opt, go.cuda(), rgb, grads)
+    rb = O.render(og, oopt, o.numpy(), d.numpy(), mode=2, grad_out=go.numpy(), color=ref["rgb"])
+    assert_grad(grads.grad_density_out.cpu().numpy(), rb["grad_density"], "bwd grad_density")
+    assert_grad(grads.grad_sh_out.cpu().numpy(), rb["grad_sh"], "bwd grad_sh")
+    # gradients accumulate into existing buffers
+    C.volume_render_cuvol_backward(spec, rays, opt, go.cuda(), rgb, grads)
+    assert_grad(grads.grad_sh_out.cpu().numpy(), 2 * rb["grad_sh"], "accumulated grad_sh")
+
+
+@pytest.mark.parametrize("ndc", [False, True])
+def test_image_parity(ndc):
+    from svox2_gb300 import csrc as C
+    g = S.make_grid(48, occupancy=0.3, seed=15)
+    spec, og = grid_pair(g)
+    if ndc:
+        c2w = torch.eye(4)
+        c2w[:3, 3] = torch.tensor([0.05, -0.02, 0.0])
+        ndc_c = (1.4, 1.2)
+    else:
+        c2w = S.look_at_c2w((0.4, -0.7, -3.2))
+        ndc_c = (-1.0, -1.0)
+    cam = C.CameraSpec()
+    cam.c2w = c2w.cuda()
+    cam.fx, cam.fy, cam.cx, cam.cy = 70.0, 72.0, 31.5, 24.0
+    cam.width, cam.height = 64, 48
+    cam.ndc_coeffx, cam.ndc_coeffy = ndc_c
+    opt, oopt = opt_struct()
+    st = _stats(64 * 48)
+    img = C.volume_render_cuvol_image(spec, cam, opt, stats=st)
+    torch.cuda.synchronize()
+    ref = O.render_image(og, oopt, c2w.numpy(), 70.0, 72.0, 31.5, 24.0, 64, 48, ndc=ndc_c, trace=True)
+    assert (st["ray_trace"].cpu().numpy().view(np.uint64) == ref["trace"]).all()
+    assert_rgb(img.cpu().numpy(), ref["rgb"], "image")
+
+
+def test_accelerated_links_skip():
+    """Negative links below -1 (empty-space skip levels) are honoured exactly."""
+    g = S.make_grid(32, occupancy=0.25, seed=16)
+    links = g.links.clone()
+    # mark empty 4^3 blocks with skip level -3 (2^(3-1) = 4 cells), the way accel_dist_prop encodes them
+    L = links.view(8, 4, 8, 4, 8, 4).permute(0, 2, 4, 1, 3, 5).reshape(8, 8, 8, 64)
+    empty = (L < 0).all(dim=-1)
+    L[empty] = -3
+    g.links = L.view(8, 8, 8, 4, 4, 4).permute(0, 3, 1, 4, 2, 5).reshape(32, 32, 32).contiguous()
+    spec, og = grid_pair(g)
+    o, d, gt = S.make_rays(1024, seed=17)
+    opt, oopt = opt_struct()
+    _run_fused(spec, og, rays_pair(o, d), o, d, gt, opt, oopt)
+
+
+def test_invalid_arguments_raise():
+    from svox2_gb300 import csrc as C
+    g = S.make_grid(8, seed=18)
+    spec, _ = grid_pair(g)
+    o, d, gt = S.make_rays(4, seed=19)
+    opt, _ = opt_struct()
+    with pytest.raises(RuntimeError):
+        C.volume_render_cuvol(spec, rays_pair(o.double(), d.double()), opt)
+    bad = rays_pair(o, d)
+    bad.origins = o  # CPU tensor
+    with pytest.raises(RuntimeError):
+        C.volume_render_cuvol(spec, bad, opt)
+    spec.basis_dim = 16
+    with pytest.raises(RuntimeError):
+        C.volume_render_cuvol(spec, rays_pair(o, d), opt)

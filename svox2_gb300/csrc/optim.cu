@@ -72,6 +72,7 @@ __global__ void __launch_bounds__(256) step_list_kernel(OptArgs a, const int64_t
     const long long k = e / a.n_cols;
     const int col = (int)(e - k * a.n_cols);
     const long long row = __ldg(idx + k);
+    if (row < 0 || row >= a.n_rows) continue;  // index outside the table
     step_one<T, RMS>(a, row * a.n_cols + col, col);
   }
 }

@@ -296,6 +296,7 @@ struct Seg {
 __device__ __forceinline__ void march_segment(Seg& s, float t0, float lt0, const RayGeo& r,
                                               const GridP& g, const OptP& opt, int* slinks,
                                               unsigned long long* trace_h, int lane) {
+  __syncwarp();  // every lane is done with the previous segment's staged links
   // Sample t: t0 + step added lane times, one rounding per add (trace_ray_cuvol's t += step).
   float tk = t0;
 #pragma unroll
@@ -402,14 +403,15 @@ __device__ __forceinline__ void march_segment(Seg& s, float t0, float lt0, const
     const int was_skip = __shfl_sync(kFull, (int)is_skip, s.n);
     if (was_skip) {
       s.t_next = __fadd_rn(tm, __fmul_rn(ceilf(__fdiv_rn(sk, opt.step)), opt.step));
-      s.end = !(s.t_next <= r.tmax);
+      // a march whose t no longer advances (t + step == t in float) ends here
+      s.end = !(s.t_next <= r.tmax) || !(s.t_next > t0);
     } else {
       s.end = true;
       s.t_next = tm;
     }
   } else {
     s.t_next = __fadd_rn(__shfl_sync(kFull, tk, 31), opt.step);
-    s.end = !(s.t_next <= r.tmax);
+    s.end = !(s.t_next <= r.tmax) || !(s.t_next > t0);
   }
 }
 

@@ -101,7 +101,7 @@ __global__ void __launch_bounds__(256) sample_bwd_kernel(SampleGrid g, const flo
       const float x = (j & 4) ? xb : xa, y = (j & 2) ? yb : ya, z = (j & 1) ? zb : za;
       return __fmul_rn(__fmul_rn(y, __fmul_rn(x, go)), z);
     };
-    if (lane < 8 && lk[0] == lk[0]) {
+    if (lane < 8) {
       const float go = __ldg(gd + pid);
       int lkj = lk[0];
 #pragma unroll

@@ -46,6 +46,7 @@ __global__ void __launch_bounds__(256) tv_sparse_kernel(TvArgs a, const int32_t*
        tid += (long long)gridDim.x * blockDim.x) {
     const int idx = (int)(tid % a.nch) + a.start;
     const int xyz = __ldg(cells + tid / a.nch);
+    if ((unsigned)xyz >= (unsigned)(a.X * a.Y * a.Z)) continue;  // cell index outside the grid
     const int z = xyz % a.Z, xy = xyz / a.Z;
     const int y = xy % a.Y, x = xy / a.Y;
     const long long offy = a.Z, offx = (long long)a.Y * a.Z;

@@ -25,7 +25,7 @@ def _stats(Q):
             "ray_trace": torch.zeros(Q, dtype=torch.int64, device="cuda")}
 
 
-def _run_fused(spec, og, rays, o, d, gt, opt, oopt, beta=0.0, sparsity=0.0, check_f64=True):
+def _run_fused(spec, og, rays, o, d, gt, opt, oopt, beta=0.0, sparsity=0.0, check_f64=True, grad_ref="f32"):
     from svox2_gb300 import csrc as C
     Q = o.shape[0]
     N = og.density.shape[0]
@@ -44,12 +44,15 @@ def _run_fused(spec, og, rays, o, d, gt, opt, oopt, beta=0.0, sparsity=0.0, chec
     assert mism == 0, f"sample indexing differs on {mism} of {Q} rays"
     assert int(st["eval_samples"].item()) == ref["n_eval"]
     assert_rgb(rgb.cpu().numpy(), ref["rgb"], "rgb")
-    assert_grad(grads.grad_density_out.cpu().numpy(), ref["grad_density"], "grad_density")
-    assert_grad(grads.grad_sh_out.cpu().numpy(), ref["grad_sh"], "grad_sh")
     np.testing.assert_array_equal(grads.mask_out.cpu().numpy(), ref["mask"])
-    if check_f64:
+    r64 = None
+    if check_f64 or grad_ref == "f64":
         r64 = O.render(og, oopt, o.numpy(), d.numpy(), mode=1, rgb_gt=gt.numpy(), beta_loss=beta,
                        sparsity_loss=sparsity, prec="f64")
+    gref = ref if grad_ref == "f32" else r64
+    assert_grad(grads.grad_density_out.cpu().numpy(), gref["grad_density"], "grad_density")
+    assert_grad(grads.grad_sh_out.cpu().numpy(), gref["grad_sh"], "grad_sh")
+    if check_f64:
         print(f"vs f64: kernel rgb {rel_err(rgb.cpu().numpy(), r64['rgb']):.2e} "
               f"gsh {rel_err(grads.grad_sh_out.cpu().numpy(), r64['grad_sh']):.2e} "
               f"gd {rel_err(grads.grad_density_out.cpu().numpy(), r64['grad_density']):.2e} | "
@@ -70,7 +73,6 @@ CASES = {
     "thresh_hi": (32, 0.4, 9, torch.float32, 768, {"sigma_thresh": 5.0, "stop_thresh": 1e-3}),
     "near_clip": (32, None, 9, torch.float32, 512, {"near_clip": 0.4}),
     "spheric_clip": (32, None, 9, torch.float32, 512, {"spheric": True, "near_clip": 0.1}),
-    "last_opaque": (32, 0.5, 9, torch.float32, 512, {"last_opaque": True}),
 }
 
 
@@ -82,6 +84,20 @@ def test_fused_parity(name):
     o, d, gt = S.make_rays(Q, seed=4)
     opt, oopt = opt_struct(**kw)
     _run_fused(spec, og, rays_pair(o, d), o, d, gt, opt, oopt)
+
+
+def test_fused_last_sample_opaque():
+    """last_sample_opaque gives the final sample a 1e9 world step.  The reference's
+    forward-order adjoint forms accum = dot(C, g) - sum(w tc), a rounding residual
+    near zero at the last sample, and multiplies it by that step: its float32
+    density gradient there is rounding noise of order 1e-2.  The reverse-order
+    adjoint accumulates the suffix sum directly (exactly 0 after an opaque
+    sample), so its gradients are checked against the float64 restatement."""
+    g = S.make_grid(32, occupancy=0.5, seed=3)
+    spec, og = grid_pair(g)
+    o, d, gt = S.make_rays(512, seed=4)
+    opt, oopt = opt_struct(last_opaque=True)
+    _run_fused(spec, og, rays_pair(o, d), o, d, gt, opt, oopt, grad_ref="f64")
 
 
 def test_fused_beta_sparsity():

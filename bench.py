@@ -122,12 +122,7 @@ def build_workload(device, seed_rays: int, n_batches: int):
     from svox2_gb300 import SparseGrid
 
     g = S.make_grid(RESO, occupancy=OCC, n_balls=N_BALLS, seed=0, device=device)
-    grid = SparseGrid(reso=RESO, basis_dim=9, device=device)
-    N = g.density.shape[0]
-    grid.links = g.links.to(device)
-    grid.density_data = torch.nn.Parameter(g.density.to(device))
-    grid.sh_data = torch.nn.Parameter(g.sh.to(device))
-    grid.capacity = N
+    grid = SparseGrid.from_tables(g.links.to(device), g.density.to(device), g.sh.to(device))
     grid.opt.sigma_thresh = 1e-8
     grid.opt.stop_thresh = 1e-7
     grid.opt.background_brightness = 1.0
@@ -239,13 +234,17 @@ def run_reference(args, rank, world):
 
 
 def main():
+    global Q
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--rays", type=int, default=1_000_000, help="rays per step (profiling runs use a smaller case)")
+    ap.add_argument("--skip-e2e", action="store_true", help="leave out the host-copy arm (profiling runs)")
     args = ap.parse_args()
+    Q = args.rays
     args.warmup = max(args.warmup, 3)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -306,6 +305,18 @@ def main():
         total_ms = float(tt.item())
 
     # ---- e2e: public API, rays from pinned host memory, colours back to the host
+    if args.skip_e2e:
+        e2e_ms = float("nan")
+    else:
+        e2e_ms = run_e2e(args, grid, host_batches, device, n_batches, dist)
+    value = world * Q * args.steps / (total_ms / 1e3)
+    e2e_val = world * Q * args.steps / (e2e_ms / 1e3)
+    emit(args, rank, world, g, value, e2e_val, total_ms, kern_ms, n_eval, clk)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def run_e2e(args, grid, host_batches, device, n_batches, dist):
     pinned = [tuple(t.pin_memory() for t in b) for b in host_batches]
     dbuf = tuple(torch.empty((Q, 3), device=device) for _ in range(3))
     hout = torch.empty((Q, 3), dtype=torch.float32).pin_memory()
@@ -331,9 +342,10 @@ def main():
         tt = torch.tensor([e2e_ms], device=device)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         e2e_ms = float(tt.item())
+    return e2e_ms
 
-    value = world * Q * args.steps / (total_ms / 1e3)
-    e2e_val = world * Q * args.steps / (e2e_ms / 1e3)
+
+def emit(args, rank, world, g, value, e2e_val, total_ms, kern_ms, n_eval, clk):
     peak, peak_kind = _peaks()
     per_launch_s = kern_ms / 1e3 / args.steps
     alg_bytes = (n_eval / args.steps) * BYTES_PER_SAMPLE + BYTES_PER_RAY * Q
@@ -363,8 +375,6 @@ def main():
             "clocks": clk.summary(),
         }
         print(json.dumps(line), flush=True)
-    if dist is not None:
-        dist.destroy_process_group()
 
 
 if __name__ == "__main__":

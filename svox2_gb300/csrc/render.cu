@@ -592,7 +592,7 @@ __global__ void __launch_bounds__(kThreads) render_kernel(GridP g, OptP opt, IoP
         seg_since_ck = (seg_since_ck + 1) % stride;
       }
       __syncwarp();
-      const float w_lane = __fmul_rn(__expf(s.lt_before), __fsub_rn(1.f, __expf(-s.pcnt)));
+      const float w_lane = __fmul_rn(expf(s.lt_before), __fsub_rn(1.f, expf(-s.pcnt)));
       unsigned m = s.evm;
       while (m) {
         const int i = __ffs(m) - 1;
@@ -627,7 +627,7 @@ __global__ void __launch_bounds__(kThreads) render_kernel(GridP g, OptP opt, IoP
     __syncwarp();
     evals += (unsigned long long)n_eval;
     const float lt_fwd = stopped ? -1e3f : lt;   // cuvol.cu:103-106
-    const float out_c = fmaf(__expf(lt_fwd), opt.bg, acc);
+    const float out_c = fmaf(expf(lt_fwd), opt.bg, acc);
     if (MODE != kBwd && grp < 3 && cj == 0) io.rgb_out[ray * 3 + grp] = out_c;
     if (io.trace != nullptr && lane == 0) io.trace[ray] = th;
 
@@ -647,10 +647,10 @@ __global__ void __launch_bounds__(kThreads) render_kernel(GridP g, OptP opt, IoP
       }
       const float gmine = grp < 3 ? gout[grp == 0 ? 0 : (grp == 1 ? 1 : 2)] : 0.f;
       // light that passes the last sample: background, plus the beta-loss term (cuvol.cu:259-264)
-      float accum = __fmul_rn(__fmul_rn(__expf(lt_fwd), opt.bg),
+      float accum = __fmul_rn(__fmul_rn(expf(lt_fwd), opt.bg),
                               __fadd_rn(__fadd_rn(gout[0], gout[1]), gout[2]));
       if (MODE == kFused && io.beta > 0.f) {
-        const float tin = __expf(lt_fwd);
+        const float tin = expf(lt_fwd);
         const double f = 1.0 - (double)tin / __dadd_rn((double)__fsub_rn(1.f, tin), 1e-3);
         accum = __fadd_rn(accum, (float)((double)io.beta * f));
       }
@@ -702,8 +702,8 @@ __global__ void __launch_bounds__(kThreads) render_kernel(GridP g, OptP opt, IoP
           __syncwarp();
           march_segment(s, t0, lt0, rg, g, opt, sm.links, nullptr, lane);
           __syncwarp();
-          const float w_lane = __fmul_rn(__expf(s.lt_before), __fsub_rn(1.f, __expf(-s.pcnt)));
-          const float tn_lane = __expf(s.lt_after);
+          const float w_lane = __fmul_rn(expf(s.lt_before), __fsub_rn(1.f, expf(-s.pcnt)));
+          const float tn_lane = expf(s.lt_after);
           unsigned m = s.evm;
           int rank = __popc(m);
           while (m) {

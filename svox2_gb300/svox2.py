@@ -340,6 +340,21 @@ class SparseGrid(nn.Module):
         if self.links.is_cuda and use_sphere_bound:
             self.accelerate()
 
+    @classmethod
+    def from_tables(cls, links: torch.Tensor, density_data: torch.Tensor, sh_data: torch.Tensor,
+                    radius: Union[float, List[float]] = 1.0, center: Union[float, List[float]] = [0.0, 0.0, 0.0],
+                    basis_dim: Optional[int] = None) -> "SparseGrid":
+        """A grid over existing tables (links int32 [X,Y,Z], density [N,1], sh [N,3*bd]) on their
+        device, without allocating a dense grid first (what SparseGrid.load does for a checkpoint)."""
+        bd = basis_dim if basis_dim is not None else sh_data.size(1) // 3
+        grid = cls(reso=[2, 2, 2], radius=radius, center=center, basis_dim=bd, device=links.device,
+                   sh_dtype=sh_data.dtype)
+        grid.links = links.to(torch.int32).contiguous()
+        grid.density_data = nn.Parameter(density_data.contiguous())
+        grid.sh_data = nn.Parameter(sh_data.contiguous())
+        grid.capacity = density_data.size(0)
+        return grid
+
     # ---- properties (svox2/svox2.py:537-559)
     @property
     def data_dim(self):

@@ -25,7 +25,11 @@ def _stats(Q):
             "ray_trace": torch.zeros(Q, dtype=torch.int64, device="cuda")}
 
 
-def _run_fused(spec, og, rays, o, d, gt, opt, oopt, beta=0.0, sparsity=0.0, check_f64=True, grad_ref="f32"):
+def _run_fused(spec, og, rays, o, d, gt, opt, oopt, beta=0.0, sparsity=0.0, check_f64=True, grad_ref="f32",
+               long_rays=False):
+    """long_rays: thousands of samples per ray summed in float32 — colours are held
+    to the float64 yardstick at twice the float32 oracle's own error instead of the
+    flat 1e-5 bound."""
     from svox2_gb300 import csrc as C
     Q = o.shape[0]
     N = og.density.shape[0]
@@ -43,12 +47,17 @@ def _run_fused(spec, og, rays, o, d, gt, opt, oopt, beta=0.0, sparsity=0.0, chec
     mism = int((k_trace != ref["trace"]).sum())
     assert mism == 0, f"sample indexing differs on {mism} of {Q} rays"
     assert int(st["eval_samples"].item()) == ref["n_eval"]
-    assert_rgb(rgb.cpu().numpy(), ref["rgb"], "rgb")
     np.testing.assert_array_equal(grads.mask_out.cpu().numpy(), ref["mask"])
     r64 = None
-    if check_f64 or grad_ref == "f64":
+    if check_f64 or grad_ref == "f64" or long_rays:
         r64 = O.render(og, oopt, o.numpy(), d.numpy(), mode=1, rgb_gt=gt.numpy(), beta_loss=beta,
                        sparsity_loss=sparsity, prec="f64")
+    if long_rays:
+        e_k = np.abs(rgb.cpu().numpy() - r64["rgb"]).max()
+        e_o = np.abs(ref["rgb"] - r64["rgb"]).max()
+        assert e_k <= 2 * e_o + 1e-6, f"long-ray colour error {e_k:.2e} vs float32 oracle's {e_o:.2e}"
+    else:
+        assert_rgb(rgb.cpu().numpy(), ref["rgb"], "rgb")
     gref = ref if grad_ref == "f32" else r64
     assert_grad(grads.grad_density_out.cpu().numpy(), gref["grad_density"], "grad_density")
     assert_grad(grads.grad_sh_out.cpu().numpy(), gref["grad_sh"], "grad_sh")
@@ -128,7 +137,7 @@ def test_long_rays_colour_cache_and_checkpoint_thinning():
     d = d / d.norm(dim=-1, keepdim=True)
     gt = torch.rand((Q, 3), generator=gen)
     opt, oopt = opt_struct(stop_thresh=0.0)
-    _, _, ref = _run_fused(spec, og, rays_pair(o, d), o, d, gt, opt, oopt)
+    _, _, ref = _run_fused(spec, og, rays_pair(o, d), o, d, gt, opt, oopt, long_rays=True)
     assert ref["n_eval"] > Q * 2500
 
 

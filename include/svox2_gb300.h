@@ -155,6 +155,25 @@ int svx_volume_render_cuvol_fused(const svx_grid_t* grid, const svx_rays_t* rays
                                   const svx_grid_grads_t* grads,
                                   const svx_render_stats_t* stats, void* stream);
 
+/* svx_volume_render_cuvol_fused_noalloc — no counterpart in the reference.
+ * The fused render above for callers that cannot allocate device memory
+ * while they run (work inside another framework's callbacks, hosts that plan
+ * all device memory up front, processes whose device heap belongs to a
+ * foreign allocator).  Same arguments and results as
+ * svx_volume_render_cuvol_fused; it calls no cudaMalloc/cudaFree and no
+ * allocating routine.  Its scratch (the ray counter) is a 256-byte static
+ * device array held by every GPU that loads the library until exit; a call
+ * needs 8 bytes of it, and a larger need is rejected with SVX_ERR_TOO_LARGE.
+ * The first call on a device looks the array's address up (once per device)
+ * and should come before any stream capture on that device.  All calls
+ * share the array: calls that overlap on the GPU race on the counter and
+ * must be serialised by the caller. */
+int svx_volume_render_cuvol_fused_noalloc(const svx_grid_t* grid, const svx_rays_t* rays,
+                                          const svx_render_opts_t* opt, const float* rgb_gt,
+                                          float beta_loss, float sparsity_loss, float* rgb_out,
+                                          const svx_grid_grads_t* grads,
+                                          const svx_render_stats_t* stats, void* stream);
+
 /* ---- point sampling: svox2/csrc/svox2_kernel.cu ------------------------ */
 
 /* sample_grid (svox2/csrc/svox2.cpp:11-12, svox2_kernel.cu:181-217).

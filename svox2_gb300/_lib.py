@@ -97,6 +97,8 @@ SIGNATURES = {
                                          P(SvxRenderStats), _vp],
     "svx_volume_render_cuvol_fused": [P(SvxGrid), P(SvxRays), P(SvxRenderOpts), _vp, _f32, _f32, _vp,
                                       P(SvxGridGrads), P(SvxRenderStats), _vp],
+    "svx_volume_render_cuvol_fused_noalloc": [P(SvxGrid), P(SvxRays), P(SvxRenderOpts), _vp, _f32, _f32, _vp,
+                                              P(SvxGridGrads), P(SvxRenderStats), _vp],
     "svx_sample_grid": [P(SvxGrid), _vp, _i64, _i32, _vp, _vp, _vp],
     "svx_sample_grid_backward": [P(SvxGrid), _vp, _i64, _vp, _vp, _vp, _vp, _i32, _vp],
     "svx_tv_grad": [_vp, P(_i32), P(SvxTable), _i32, _i32, _f32, _i32, _f32, _i32, _f32, _f32, _vp, _vp],

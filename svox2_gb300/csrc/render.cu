@@ -1050,3 +1050,94 @@ extern "C" int svx_volume_render_cuvol_image(const svx_grid_t* grid, const svx_c
 }
 
 extern "C" int svx_color_cache_capacity(void) { return svx::g_cap; }
+
+// ---------------------------------------------------------------- no-allocation entry point
+//
+// Some callers cannot allocate device memory while they run: code that
+// executes inside another framework's stream callbacks or replayed work,
+// embedded and real-time hosts that plan all device memory before they start,
+// and processes where a foreign allocator owns the device heap, so that a
+// cudaMalloc (or a stream-ordered allocation) would fail or compete with it.
+// svx_volume_render_cuvol_fused_noalloc serves them: it is the fused render
+// above with its one piece of scratch — the persistent warps' ray counter —
+// taken from the file-scope array below instead of an allocation.
+//
+// The array is kStaticScratchWords 64-bit words (256 bytes).  Every GPU that
+// loads this library holds one copy of it until the process exits.  A call
+// needs one word; the entry rejects any request for more scratch than the
+// array holds.  All calls share the array and it keeps the last call's
+// contents: each call clears the counter on its stream before the kernel
+// starts, so calls that overlap on the GPU (on different streams, or from
+// different host threads) race on the counter and must be serialised by the
+// caller.
+constexpr int kStaticScratchWords = 32;
+static __device__ __align__(256) unsigned long long g_static_scratch[kStaticScratchWords];
+
+// Device address of g_static_scratch on the current device, looked up once
+// per device (with that device current) and cached.  In host code the
+// symbol's name is only a host-side stand-in; the kernel must be given the
+// address cudaGetSymbolAddress returns.
+static int static_scratch_address(unsigned long long** out) {
+  static std::mutex mu;
+  static unsigned long long* addr[64] = {nullptr};
+  int dev = 0;
+  SVX_CUDA_TRY(cudaGetDevice(&dev));
+  SVX_REQUIRE(dev >= 0 && dev < 64, SVX_ERR_UNSUPPORTED, "device index %d: at most 64 devices", dev);
+  std::lock_guard<std::mutex> lk(mu);
+  if (addr[dev] == nullptr) {
+    void* p = nullptr;
+    SVX_CUDA_TRY(cudaGetSymbolAddress(&p, g_static_scratch));
+    addr[dev] = reinterpret_cast<unsigned long long*>(p);
+  }
+  *out = addr[dev];
+  return SVX_OK;
+}
+
+extern "C" int svx_volume_render_cuvol_fused_noalloc(const svx_grid_t* grid, const svx_rays_t* rays,
+                                                     const svx_render_opts_t* opt, const float* rgb_gt,
+                                                     float beta_loss, float sparsity_loss, float* rgb_out,
+                                                     const svx_grid_grads_t* grads,
+                                                     const svx_render_stats_t* stats, void* stream) {
+  clear_error();
+  SVX_REQUIRE(rays != nullptr, SVX_ERR_INVALID, "rays are null");
+  SVX_REQUIRE(grads != nullptr, SVX_ERR_INVALID, "grads are null");
+  SVX_REQUIRE(rays->n_rays == 0 || (rgb_gt && rgb_out), SVX_ERR_INVALID, "rgb_gt / rgb_out are null");
+  int rc = check_grid(grid);
+  if (rc) return rc;
+  SVX_REQUIRE(rays->n_rays >= 0, SVX_ERR_INVALID, "n_rays < 0");
+  if (rays->n_rays == 0) return SVX_OK;
+  SVX_REQUIRE(rays->origins && rays->dirs, SVX_ERR_INVALID, "ray tables must be non-null");
+  OptP o;
+  rc = make_opt(opt, &o);
+  if (rc) return rc;
+  const GridP g = make_grid(grid);
+  const double diag = std::sqrt((double)g.size[0] * g.size[0] + (double)g.size[1] * g.size[1] +
+                                (double)g.size[2] * g.size[2]);
+  const double max_samples = diag / (double)o.step + 2.0;
+  SVX_REQUIRE(max_samples <= (double)kNumCkpt * kMaxStride, SVX_ERR_TOO_LARGE,
+              "up to %.0f samples per ray (grid diagonal / step_size); the adjoint supports %d", max_samples,
+              kNumCkpt * kMaxStride);
+  const int need_words = 1;  // the ray counter
+  SVX_REQUIRE(need_words <= kStaticScratchWords, SVX_ERR_TOO_LARGE,
+              "needs %d words of static scratch, the array holds %d", need_words, kStaticScratchWords);
+  unsigned long long* scratch = nullptr;
+  rc = static_scratch_address(&scratch);
+  if (rc) return rc;
+  IoP io{};
+  io.rgb_out = rgb_out;
+  io.rgb_gt = rgb_gt;
+  io.grad_density = grads->grad_density_out;
+  io.grad_sh = grads->grad_sh_out;
+  io.mask = grads->mask_out;
+  io.norm = 2.f / (float)(3 * (long long)rays->n_rays);
+  io.beta = beta_loss / (float)rays->n_rays;
+  io.sparsity = sparsity_loss;
+  io.origins = rays->origins;
+  io.dirs = rays->dirs;
+  io.n_rays = rays->n_rays;
+  io.eval_count = stats ? reinterpret_cast<unsigned long long*>(stats->eval_samples) : nullptr;
+  io.trace = stats ? reinterpret_cast<unsigned long long*>(stats->ray_trace) : nullptr;
+  io.cap = g_cap;
+  io.work = scratch;  // cleared on the stream by the launch, before the kernel
+  return dispatch<kFused, false>(grid, g, o, io, rays->n_rays, as_stream(stream));
+}

@@ -27,9 +27,10 @@ def _stats(Q):
 
 def _run_fused(spec, og, rays, o, d, gt, opt, oopt, beta=0.0, sparsity=0.0, check_f64=True, grad_ref="f32",
                long_rays=False):
-    """long_rays: thousands of samples per ray summed in float32 — colours are held
-    to the float64 yardstick at twice the float32 oracle's own error instead of the
-    flat 1e-5 bound."""
+    """long_rays: thousands of samples per ray summed in float32 — colours and
+    gradients are held to the float64 yardstick at twice the float32 oracle's own
+    error instead of the flat 1e-5 bound (the oracle keeps the reference's
+    1 - exp(-x) weight, which loses digits on such thin media)."""
     from svox2_gb300 import csrc as C
     Q = o.shape[0]
     N = og.density.shape[0]
@@ -59,8 +60,14 @@ def _run_fused(spec, og, rays, o, d, gt, opt, oopt, beta=0.0, sparsity=0.0, chec
     else:
         assert_rgb(rgb.cpu().numpy(), ref["rgb"], "rgb")
     gref = ref if grad_ref == "f32" else r64
-    assert_grad(grads.grad_density_out.cpu().numpy(), gref["grad_density"], "grad_density")
-    assert_grad(grads.grad_sh_out.cpu().numpy(), gref["grad_sh"], "grad_sh")
+    if long_rays:
+        for key, k in (("grad_density", grads.grad_density_out), ("grad_sh", grads.grad_sh_out)):
+            e_k = rel_err(k.cpu().numpy(), r64[key])
+            e_o = rel_err(ref[key], r64[key])
+            assert e_k <= 2 * e_o + 1e-6, f"long-ray {key} error {e_k:.2e} vs float32 oracle's {e_o:.2e}"
+    else:
+        assert_grad(grads.grad_density_out.cpu().numpy(), gref["grad_density"], "grad_density")
+        assert_grad(grads.grad_sh_out.cpu().numpy(), gref["grad_sh"], "grad_sh")
     if check_f64:
         print(f"vs f64: kernel rgb {rel_err(rgb.cpu().numpy(), r64['rgb']):.2e} "
               f"gsh {rel_err(grads.grad_sh_out.cpu().numpy(), r64['grad_sh']):.2e} "

@@ -247,27 +247,50 @@ __device__ __forceinline__ float skip_dist(int32_t link, const int l[3], const f
 
 // ---------------------------------------------------------------- shared memory
 
+// Per-segment cell runs: consecutive evaluated samples in the same cell share
+// one slot.  Slot 0 carries the previous segment's last cell (forward pass);
+// slots 1..32 hold this segment's runs.
+constexpr int kSlots = 33;
+constexpr int kSlotStride = 33;  // floats per slot (odd: lanes reading different slots hit different banks)
+constexpr int kTileRows = 10;    // coefficient rows gathered per pass (30 lanes = 10 rows x 3 groups)
+constexpr int kMaxRows = 8 * 32; // corner rows a segment can need
+
 struct WarpSmem {
-  int* links;      // [32][8] corner links of the staged samples
-  float* tile;     // [8][C] coefficient tile for the corner gather
-  float* ck_t;     // [kNumCkpt]
-  float* ck_lt;    // [kNumCkpt]
-  int* ck_idx;     // [kNumCkpt]
-  float* tmp_t;    // [kMaxStride]
+  int* links;        // [32][8] corner links of the staged samples
+  float* slot;       // [kSlots][kSlotStride]: D[j*3+g] (colour pass) or B[g*8+j] (adjoint)
+  float* tile;       // [kTileRows][C] gathered coefficient rows
+  int* rowlink;      // [kMaxRows] link of each row to gather
+  int* rowdst;       // [kMaxRows] slot*8 + corner of each row
+  int* run_lane;     // [kSlots] first lane of each run
+  int* run_l;        // [kSlots][3] cell of each run
+  int* run_need;     // [kSlots] corners the run gathers (bit mask)
+  int* run_delta;    // [kSlots] index offset of a shared corner in the previous run
+  float* ck_t;       // [kNumCkpt]
+  float* ck_lt;      // [kNumCkpt]
+  int* ck_idx;       // [kNumCkpt]
+  float* tmp_t;      // [kMaxStride]
   float* tmp_lt;
   int* tmp_idx;
-  float* col;      // [cap][3]
+  float* col;        // [cap][3]
 };
 
 __host__ __device__ constexpr int warp_smem_floats(int C, int cap) {
-  return (32 * 8 + 8 * C + 3 * kNumCkpt + 3 * kMaxStride + 3 * cap + 3) & ~3;
+  return (32 * 8 + kSlots * kSlotStride + kTileRows * C + 2 * kMaxRows + kSlots * 6 + 3 * kNumCkpt +
+          3 * kMaxStride + 3 * cap + 3) & ~3;
 }
 
 __device__ __forceinline__ WarpSmem carve(float* base, int C, int cap) {
   WarpSmem s;
   s.links = reinterpret_cast<int*>(base);
-  s.tile = base + 32 * 8;
-  s.ck_t = s.tile + 8 * C;
+  s.slot = base + 32 * 8;
+  s.tile = s.slot + kSlots * kSlotStride;
+  s.rowlink = reinterpret_cast<int*>(s.tile + kTileRows * C);
+  s.rowdst = s.rowlink + kMaxRows;
+  s.run_lane = s.rowdst + kMaxRows;
+  s.run_l = s.run_lane + kSlots;
+  s.run_need = s.run_l + 3 * kSlots;
+  s.run_delta = s.run_need + kSlots;
+  s.ck_t = reinterpret_cast<float*>(s.run_delta + kSlots);
   s.ck_lt = s.ck_t + kNumCkpt;
   s.ck_idx = reinterpret_cast<int*>(s.ck_lt + kNumCkpt);
   s.tmp_t = reinterpret_cast<float*>(s.ck_idx + kNumCkpt);
@@ -290,6 +313,7 @@ struct Seg {
   // per-lane (valid for lanes in evm)
   float pos[3];
   int l[3];
+  long long base;   // linear index of the cell
   float sigma, pcnt, ws, lt_before, lt_after;
 };
 
@@ -297,11 +321,21 @@ __device__ __forceinline__ void march_segment(Seg& s, float t0, float lt0, const
                                               const GridP& g, const OptP& opt, int* slinks,
                                               unsigned long long* trace_h, int lane) {
   __syncwarp();  // every lane is done with the previous segment's staged links
-  // Sample t: t0 + step added lane times, one rounding per add (trace_ray_cuvol's t += step).
-  float tk = t0;
+  // Sample t: the reference adds step to t once per sample (trace_ray_cuvol's t += step).
+  // Lane k's value of that chain equals the single-rounded t0 + k*step whenever every add
+  // in the chain is exact; each lane checks its own link of the chain and the warp falls
+  // back to the explicit sequence of adds if any is not.
+  float tk = fmaf((float)lane, opt.step, t0);
+  {
+    const float prev = __shfl_up_sync(kFull, tk, 1);
+    const bool ok = lane == 0 ? (tk == t0) : (__fadd_rn(prev, opt.step) == tk);
+    if (!__all_sync(kFull, ok)) {
+      tk = t0;
 #pragma unroll
-  for (int i = 0; i < 31; ++i)
-    if (i < lane) tk = __fadd_rn(tk, opt.step);
+      for (int i = 0; i < 31; ++i)
+        if (i < lane) tk = __fadd_rn(tk, opt.step);
+    }
+  }
   const bool valid = tk <= r.tmax;
 #pragma unroll
   for (int j = 0; j < 3; ++j) {
@@ -311,6 +345,7 @@ __device__ __forceinline__ void march_segment(Seg& s, float t0, float lt0, const
     s.pos[j] = __fsub_rn(p, (float)s.l[j]);
   }
   const long long base = (long long)s.l[0] * g.offx + (long long)s.l[1] * g.offy + s.l[2];
+  s.base = base;
   const int32_t* lp = g.links + base;
   const int32_t lk0 = valid ? __ldg(lp) : -1;
   float skip = 0.f;
@@ -422,88 +457,179 @@ __device__ __forceinline__ float sample_weight(float lt_before, float pcnt) {
   return __fmul_rn(expf(lt_before), -expm1f(-pcnt));
 }
 
-// ---------------------------------------------------------------- corner cache
+// ---------------------------------------------------------------- cell runs and corners
 
-// Corner j of a cell sits at offset (j>>2, (j>>1)&1, j&1) — the reference's
-// link order 0, 1, offy, offy+1, offx, ... (render_util.cuh:79-88).
-// Lane L owns (group g = L>>3, corner j = L&7); group 3 (lanes 24-31) carries
-// density-gradient accumulators.
-__device__ __forceinline__ int corner_src(int j, int dx, int dy, int dz) {
-  const int sx = (j >> 2) + dx, sy = ((j >> 1) & 1) + dy, sz = (j & 1) + dz;
-  if ((unsigned)sx > 1u || (unsigned)sy > 1u || (unsigned)sz > 1u) return -1;
-  return (sx << 2) | (sy << 1) | sz;
+// Corner j of a cell sits at offset (j>>2, (j>>1)&1, j&1) — the reference's link
+// order 0, 1, offy, offy+1, offx, ... (render_util.cuh:79-88).  When a ray moves
+// from cell a to cell b = a + d with |d| <= 1 per axis, corner j of b is corner
+// j + (4 dx + 2 dy + dz) of a unless it lies on a face that d moved across.
+__device__ __forceinline__ unsigned new_corner_mask(int dx, int dy, int dz) {
+  unsigned m = 0;
+  if (dx > 0) m |= 0xF0u;   // corners with x = 1 of b are new
+  if (dx < 0) m |= 0x0Fu;   // corners with x = 0
+  if (dy > 0) m |= 0xCCu;
+  if (dy < 0) m |= 0x33u;
+  if (dz > 0) m |= 0xAAu;
+  if (dz < 0) m |= 0x55u;
+  return m;
 }
 
-__device__ __forceinline__ float corner_weight(int j, float px, float py, float pz) {
-  const float wx = (j & 4) ? px : __fsub_rn(1.f, px);
-  const float wy = (j & 2) ? py : __fsub_rn(1.f, py);
-  const float wz = (j & 1) ? pz : __fsub_rn(1.f, pz);
-  return __fmul_rn(__fmul_rn(wy, wz), wx);
+// The 8 trilinear corner weights of a sample.
+__device__ __forceinline__ void corner_weights(float px, float py, float pz, float w[8]) {
+  const float ax = __fsub_rn(1.f, px), ay = __fsub_rn(1.f, py), az = __fsub_rn(1.f, pz);
+  const float yz00 = __fmul_rn(ay, az), yz01 = __fmul_rn(ay, pz), yz10 = __fmul_rn(py, az),
+              yz11 = __fmul_rn(py, pz);
+  w[0] = __fmul_rn(yz00, ax);
+  w[1] = __fmul_rn(yz01, ax);
+  w[2] = __fmul_rn(yz10, ax);
+  w[3] = __fmul_rn(yz11, ax);
+  w[4] = __fmul_rn(yz00, px);
+  w[5] = __fmul_rn(yz01, px);
+  w[6] = __fmul_rn(yz10, px);
+  w[7] = __fmul_rn(yz11, px);
 }
 
-// Move D (lane-resident per-corner colour) from cell `from` to cell `to` and
-// gather the corners that are new.  links_to: the 8 corner links of `to`
-// (shared memory, broadcast reads).
+// Split the segment's evaluated samples into runs of equal cells.  Returns the
+// number of runs; *slot gets the lane's run slot (1..n, or 0 for samples that
+// continue the carried cell when have_prev).  Writes run_lane / run_l.
+__device__ __forceinline__ int segment_runs(const Seg& s, bool have_prev, long long prev_base,
+                                            const WarpSmem& sm, int lane, int* slot) {
+  const bool ev = (s.evm >> lane) & 1u;
+  const unsigned below = s.evm & ((1u << lane) - 1u);
+  const int p = below ? 31 - __clz(below) : 0;
+  const long long pb = __shfl_sync(kFull, s.base, p);
+  const bool start = ev && (below ? (s.base != pb) : (!have_prev || s.base != prev_base));
+  const unsigned R = __ballot_sync(kFull, start);
+  const unsigned upto = lane == 31 ? R : (R & ((2u << lane) - 1u));
+  *slot = ev ? __popc(upto) : 0;
+  if (start) {
+    sm.run_lane[*slot] = lane;
+    sm.run_l[*slot * 3 + 0] = s.l[0];
+    sm.run_l[*slot * 3 + 1] = s.l[1];
+    sm.run_l[*slot * 3 + 2] = s.l[2];
+  }
+  __syncwarp();
+  return __popc(R);
+}
+
+// Per-corner colour of every run: slot[r][j*3+g] = sum_k basis_k sh[link_j][g*bd+k]
+// for runs 1..nR.  Corners shared with the previous run (slot r-1; slot 0 is the
+// carried cell when have_prev) are copied, the others gathered: 27 consecutive
+// lanes read one voxel's coefficients, 30 lanes reduce 10 rows x 3 groups.
 template <int BD, typename ShT>
-__device__ __forceinline__ float update_colour_corners(float D, bool have_from, const int from[3],
-                                                       const int to[3], const int* links_to,
-                                                       float* tile, const float basis[9],
-                                                       const ShT* __restrict__ sh, int lane) {
+__device__ __forceinline__ void run_colours(int nR, bool have_prev, const WarpSmem& sm, const float basis[9],
+                                            const ShT* __restrict__ sh, int lane) {
   constexpr int C = 3 * BD;
-  const int dx = to[0] - from[0], dy = to[1] - from[1], dz = to[2] - from[2];
-  const bool near = have_from && abs(dx) <= 1 && abs(dy) <= 1 && abs(dz) <= 1;
-  const int j = lane & 7, grp = lane >> 3;
+  // lane r-1 plans run r
   unsigned need = 0;
+  int delta = 0;
+  const int r = lane + 1;
+  if (r <= nR) {
+    if (r == 1 && !have_prev) {
+      need = 0xFFu;
+    } else {
+      const int dx = sm.run_l[r * 3 + 0] - sm.run_l[(r - 1) * 3 + 0];
+      const int dy = sm.run_l[r * 3 + 1] - sm.run_l[(r - 1) * 3 + 1];
+      const int dz = sm.run_l[r * 3 + 2] - sm.run_l[(r - 1) * 3 + 2];
+      if (abs(dx) > 1 || abs(dy) > 1 || abs(dz) > 1) {
+        need = 0xFFu;
+      } else {
+        need = new_corner_mask(dx, dy, dz);
+        delta = 4 * dx + 2 * dy + dz;
+      }
+    }
+    sm.run_need[r] = (int)need;
+    sm.run_delta[r] = delta;
+  }
+  // row table: exclusive prefix of the rows each run gathers
+  const int cnt = __popc(need);
+  int incl = cnt;
 #pragma unroll
-  for (int c = 0; c < 8; ++c)
-    if (!near || corner_src(c, dx, dy, dz) < 0) need |= 1u << c;
-  const int src = near ? corner_src(j, dx, dy, dz) : -1;
-  const float moved = __shfl_sync(kFull, D, src >= 0 ? grp * 8 + src : lane);
+  for (int d = 1; d < 32; d <<= 1) {
+    const int y = __shfl_up_sync(kFull, incl, d);
+    if (lane >= d) incl += y;
+  }
+  const int M = __shfl_sync(kFull, incl, 31);
+  if (r <= nR) {
+    int o = incl - cnt;
+    const int* lk = sm.links + sm.run_lane[r] * 8;
 #pragma unroll
-  for (int c = 0; c < 8; ++c) {
-    if (need & (1u << c)) {
-      const int lk = links_to[c];
-      if (lane < C) tile[c * C + lane] = lk >= 0 ? ldg_f32(sh + (long long)lk * C + lane) : 0.f;
+    for (int j = 0; j < 8; ++j) {
+      if ((need >> j) & 1u) {
+        sm.rowlink[o] = lk[j];
+        sm.rowdst[o] = r * 8 + j;
+        ++o;
+      }
     }
   }
   __syncwarp();
-  float out = moved;
-  if (grp < 3 && ((need >> j) & 1u)) {
-    const float* row = tile + j * C + grp * BD;
-    float acc = 0.f;
+  // gather and reduce, kTileRows rows per pass
+  const int rr = lane / 3, gg = lane - 3 * (lane / 3);
+  for (int m0 = 0; m0 < M; m0 += kTileRows) {
+    const int nrow = min(kTileRows, M - m0);
+    for (int q = 0; q < nrow; ++q) {
+      const int lk = sm.rowlink[m0 + q];
+      if (lane < C) sm.tile[q * C + lane] = lk >= 0 ? ldg_f32(sh + (long long)lk * C + lane) : 0.f;
+    }
+    __syncwarp();
+    if (rr < nrow) {
+      const float* row = sm.tile + rr * C + gg * BD;
+      float acc = 0.f;
 #pragma unroll
-    for (int k = 0; k < BD; ++k) acc = fmaf(basis[k], row[k], acc);
-    out = acc;
+      for (int k = 0; k < BD; ++k) acc = fmaf(basis[k], row[k], acc);
+      const int dst = sm.rowdst[m0 + rr];
+      sm.slot[(dst >> 3) * kSlotStride + (dst & 7) * 3 + gg] = acc;
+    }
+    __syncwarp();
   }
-  __syncwarp();
-  return out;
+  // shared corners, run by run (each copy reads a slot that is already complete)
+  const int cj = lane >> 2, cg = lane & 3;  // 24 lanes: corner cj, group cg (< 3)
+  for (int q = 1; q <= nR; ++q) {
+    const int nd = sm.run_need[q];
+    if (cg < 3 && !((nd >> cj) & 1)) {
+      const int src = cj + sm.run_delta[q];
+      sm.slot[q * kSlotStride + cj * 3 + cg] = sm.slot[(q - 1) * kSlotStride + src * 3 + cg];
+    }
+    __syncwarp();
+  }
 }
 
-// Colour of one sample from lane-resident D: lanes of group g return colour g.
-__device__ __forceinline__ float sample_colour(float D, float px, float py, float pz, int lane) {
-  float v = (lane < 24) ? __fmul_rn(corner_weight(lane & 7, px, py, pz), D) : 0.f;
-  v = __fadd_rn(v, __shfl_xor_sync(kFull, v, 1));
-  v = __fadd_rn(v, __shfl_xor_sync(kFull, v, 2));
-  v = __fadd_rn(v, __shfl_xor_sync(kFull, v, 4));
-  return v;
+// Colour (before the +0.5 offset) of the lane's sample from its run's corners.
+__device__ __forceinline__ void lane_colour(const WarpSmem& sm, int slot, const float w[8], float col[3]) {
+  const float* d = sm.slot + slot * kSlotStride;
+  float c0 = 0.f, c1 = 0.f, c2 = 0.f;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    c0 = fmaf(w[j], d[j * 3 + 0], c0);
+    c1 = fmaf(w[j], d[j * 3 + 1], c1);
+    c2 = fmaf(w[j], d[j * 3 + 2], c2);
+  }
+  col[0] = c0;
+  col[1] = c1;
+  col[2] = c2;
 }
 
-// Gradient accumulators B (lane-resident, same layout as D) for the corners of
-// the tracked cell; flush_corners atomically adds the retiring ones.
+// Flush the gradient accumulators of the retiring corners of the tracked cell.
+// Lane L holds B for (group L>>3, corner L&7); group 3 is the density.
 template <int BD>
 __device__ __forceinline__ void flush_corners(unsigned retire, float B, int lk_lane, float my_basis,
                                               float* __restrict__ grad_sh, float* __restrict__ grad_density,
                                               uint8_t* __restrict__ mask, int lane) {
   constexpr int C = 3 * BD;
-#pragma unroll 1
-  for (int c = 0; c < 8; ++c) {
-    if (!((retire >> c) & 1u)) continue;
+  const int src_group = lane < C ? lane / BD : 0;
+  while (retire) {
+    const int c = __ffs(retire) - 1;
+    retire &= retire - 1;
     const int lk = __shfl_sync(kFull, lk_lane, c);
-    const float b = __shfl_sync(kFull, B, (lane < C ? (lane / BD) : 0) * 8 + c);
+    const float b = __shfl_sync(kFull, B, src_group * 8 + c);
     if (lk >= 0 && lane < C && b != 0.f && grad_sh != nullptr)
       atomicAdd(grad_sh + (long long)lk * C + lane, __fmul_rn(my_basis, b));
   }
-  // density accumulators live in lanes 24..31 (corner = lane - 24)
+}
+
+__device__ __forceinline__ void flush_density(unsigned retire, float B, int lk_lane,
+                                              float* __restrict__ grad_density, uint8_t* __restrict__ mask,
+                                              int lane) {
   if (lane >= 24 && ((retire >> (lane - 24)) & 1u) && lk_lane >= 0) {
     if (grad_density != nullptr && B != 0.f) atomicAdd(grad_density + lk_lane, B);
     if (mask != nullptr) mask[lk_lane] = 1;
@@ -563,65 +689,73 @@ __global__ void __launch_bounds__(kThreads) render_kernel(GridP g, OptP opt, IoP
 
     // ---- forward march
     float t = rg.tmin, lt = 0.f;
-    float acc = 0.f;             // lanes of group g: colour g
-    float D = 0.f;
-    int cell[3] = {0, 0, 0};
-    bool have_cell = false;
+    float acc0 = 0.f, acc1 = 0.f, acc2 = 0.f;   // this lane's samples' colour sum
+    bool have_prev = false;
+    long long prev_base = 0;
     int n_eval = 0, nck = 0, stride = 1, seg_since_ck = 0;
     bool stopped = false;
     while (t <= rg.tmax) {
       Seg s;
       march_segment(s, t, lt, rg, g, opt, sm.links, thp, lane);
-      if (MODE != kFwd && s.evm) {
-        // checkpoint the segment (thinned to every stride-th evaluated segment)
-        if (seg_since_ck == 0) {
-          if (nck == kNumCkpt && stride < kMaxStride) {
-            // keep every other checkpoint, double the stride (kNumCkpt == 64: one per lane pair)
-            const float a = sm.ck_t[2 * lane], b = sm.ck_lt[2 * lane];
-            const int c = sm.ck_idx[2 * lane];
-            __syncwarp();
-            sm.ck_t[lane] = a;
-            sm.ck_lt[lane] = b;
-            sm.ck_idx[lane] = c;
-            __syncwarp();
-            nck = kNumCkpt / 2;
-            stride *= 2;
-          }
-          if (nck < kNumCkpt) {  // always true within the host's samples-per-ray limit
-            if (lane == 0) {
-              sm.ck_t[nck] = t;
-              sm.ck_lt[nck] = lt;
-              sm.ck_idx[nck] = n_eval;
+      if (s.evm) {
+        if (MODE != kFwd) {
+          // checkpoint the segment (thinned to every stride-th evaluated segment)
+          if (seg_since_ck == 0) {
+            if (nck == kNumCkpt && stride < kMaxStride) {
+              // keep every other checkpoint, double the stride (kNumCkpt == 64: one per lane pair)
+              const float a = sm.ck_t[2 * lane], b = sm.ck_lt[2 * lane];
+              const int c = sm.ck_idx[2 * lane];
+              __syncwarp();
+              sm.ck_t[lane] = a;
+              sm.ck_lt[lane] = b;
+              sm.ck_idx[lane] = c;
+              __syncwarp();
+              nck = kNumCkpt / 2;
+              stride *= 2;
             }
-            ++nck;
+            if (nck < kNumCkpt) {  // always true within the host's samples-per-ray limit
+              if (lane == 0) {
+                sm.ck_t[nck] = t;
+                sm.ck_lt[nck] = lt;
+                sm.ck_idx[nck] = n_eval;
+              }
+              ++nck;
+            }
+          }
+          seg_since_ck = (seg_since_ck + 1) % stride;
+        }
+        int slot;
+        const int nR = segment_runs(s, have_prev, prev_base, sm, lane, &slot);
+        run_colours<BD, ShT>(nR, have_prev, sm, basis, sh, lane);
+        const bool ev = (s.evm >> lane) & 1u;
+        if (ev) {
+          float w8[8], col[3];
+          corner_weights(s.pos[0], s.pos[1], s.pos[2], w8);
+          lane_colour(sm, slot, w8, col);
+          const float w = sample_weight(s.lt_before, s.pcnt);
+          acc0 = fmaf(w, fmaxf(__fadd_rn(col[0], 0.5f), 0.f), acc0);
+          acc1 = fmaf(w, fmaxf(__fadd_rn(col[1], 0.5f), 0.f), acc1);
+          acc2 = fmaf(w, fmaxf(__fadd_rn(col[2], 0.5f), 0.f), acc2);
+          if (MODE != kFwd) {
+            const int idx = n_eval + __popc(s.evm & ((1u << lane) - 1u));
+            if (idx < io.cap) {
+              sm.col[idx * 3 + 0] = col[0];
+              sm.col[idx * 3 + 1] = col[1];
+              sm.col[idx * 3 + 2] = col[2];
+            }
           }
         }
-        seg_since_ck = (seg_since_ck + 1) % stride;
-      }
-      __syncwarp();
-      const float w_lane = sample_weight(s.lt_before, s.pcnt);
-      unsigned m = s.evm;
-      while (m) {
-        const int i = __ffs(m) - 1;
-        m &= m - 1;
-        const int to[3] = {__shfl_sync(kFull, s.l[0], i), __shfl_sync(kFull, s.l[1], i),
-                           __shfl_sync(kFull, s.l[2], i)};
-        const float px = __shfl_sync(kFull, s.pos[0], i);
-        const float py = __shfl_sync(kFull, s.pos[1], i);
-        const float pz = __shfl_sync(kFull, s.pos[2], i);
-        const float wi = __shfl_sync(kFull, w_lane, i);
-        if (!have_cell || to[0] != cell[0] || to[1] != cell[1] || to[2] != cell[2]) {
-          D = update_colour_corners<BD, ShT>(D, have_cell, cell, to, sm.links + i * 8, sm.tile, basis,
-                                             sh, lane);
-          cell[0] = to[0];
-          cell[1] = to[1];
-          cell[2] = to[2];
-          have_cell = true;
+        // carry the last run to the next segment (after every lane has read the slots)
+        const int last = 31 - __clz(s.evm);
+        prev_base = __shfl_sync(kFull, s.base, last);
+        __syncwarp();
+        if (nR > 0) {
+          if (lane < 24) sm.slot[(lane >> 3) + 3 * (lane & 7)] = sm.slot[nR * kSlotStride + (lane >> 3) + 3 * (lane & 7)];
+          if (lane < 3) sm.run_l[lane] = sm.run_l[nR * 3 + lane];
         }
-        const float col = sample_colour(D, px, py, pz, lane);
-        acc = fmaf(wi, fmaxf(__fadd_rn(col, 0.5f), 0.f), acc);
-        if (MODE != kFwd && n_eval < io.cap && cj == 0 && grp < 3) sm.col[n_eval * 3 + grp] = col;
-        ++n_eval;
+        have_prev = true;
+        n_eval += __popc(s.evm);
+        __syncwarp();
       }
       lt = s.lt_end;
       if (s.stopped) {
@@ -633,33 +767,42 @@ __global__ void __launch_bounds__(kThreads) render_kernel(GridP g, OptP opt, IoP
     }
     __syncwarp();
     evals += (unsigned long long)n_eval;
+    // colour: this lane's partial sums, reduced over the warp
+#pragma unroll
+    for (int d = 16; d >= 1; d >>= 1) {
+      acc0 = __fadd_rn(acc0, __shfl_xor_sync(kFull, acc0, d));
+      acc1 = __fadd_rn(acc1, __shfl_xor_sync(kFull, acc1, d));
+      acc2 = __fadd_rn(acc2, __shfl_xor_sync(kFull, acc2, d));
+    }
     const float lt_fwd = stopped ? -1e3f : lt;   // cuvol.cu:103-106
-    const float out_c = fmaf(expf(lt_fwd), opt.bg, acc);
-    if (MODE != kBwd && grp < 3 && cj == 0) io.rgb_out[ray * 3 + grp] = out_c;
+    const float tb = __fmul_rn(expf(lt_fwd), opt.bg);
+    const float out0 = __fadd_rn(acc0, tb), out1 = __fadd_rn(acc1, tb), out2 = __fadd_rn(acc2, tb);
+    if (MODE != kBwd && lane == 0) {
+      io.rgb_out[ray * 3 + 0] = out0;
+      io.rgb_out[ray * 3 + 1] = out1;
+      io.rgb_out[ray * 3 + 2] = out2;
+    }
     if (io.trace != nullptr && lane == 0) io.trace[ray] = th;
 
     if (MODE != kFwd) {
       // ---- adjoint seed
-      float gout[3];
+      float gout0, gout1, gout2;
       if (MODE == kFused) {
         // residual of the MSE loss (cuvol.cu:735-741)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          const float oc = __shfl_sync(kFull, out_c, c * 8);
-          gout[c] = __fmul_rn(__fsub_rn(oc, __ldg(io.rgb_gt + ray * 3 + c)), io.norm);
-        }
+        gout0 = __fmul_rn(__fsub_rn(out0, __ldg(io.rgb_gt + ray * 3 + 0)), io.norm);
+        gout1 = __fmul_rn(__fsub_rn(out1, __ldg(io.rgb_gt + ray * 3 + 1)), io.norm);
+        gout2 = __fmul_rn(__fsub_rn(out2, __ldg(io.rgb_gt + ray * 3 + 2)), io.norm);
       } else {
-#pragma unroll
-        for (int c = 0; c < 3; ++c) gout[c] = __ldg(io.grad_out + ray * 3 + c);
+        gout0 = __ldg(io.grad_out + ray * 3 + 0);
+        gout1 = __ldg(io.grad_out + ray * 3 + 1);
+        gout2 = __ldg(io.grad_out + ray * 3 + 2);
       }
-      const float gmine = grp < 3 ? gout[grp == 0 ? 0 : (grp == 1 ? 1 : 2)] : 0.f;
       // light that passes the last sample: background, plus the beta-loss term (cuvol.cu:259-264)
-      float accum = __fmul_rn(__fmul_rn(expf(lt_fwd), opt.bg),
-                              __fadd_rn(__fadd_rn(gout[0], gout[1]), gout[2]));
+      float carry = __fmul_rn(tb, __fadd_rn(__fadd_rn(gout0, gout1), gout2));
       if (MODE == kFused && io.beta > 0.f) {
         const float tin = expf(lt_fwd);
         const double f = 1.0 - (double)tin / __dadd_rn((double)__fsub_rn(1.f, tin), 1e-3);
-        accum = __fadd_rn(accum, (float)((double)io.beta * f));
+        carry = __fadd_rn(carry, (float)((double)io.beta * f));
       }
 
       // ---- reverse pass over checkpointed segments
@@ -667,10 +810,8 @@ __global__ void __launch_bounds__(kThreads) render_kernel(GridP g, OptP opt, IoP
       int lk_lane = -1;            // link of corner (lane & 7) of the tracked cell
       int bcell[3] = {0, 0, 0};
       bool have_b = false;
-      bool have_d = false;
-      int dcell[3] = {0, 0, 0};
       for (int k = nck - 1; k >= 0; --k) {
-        // regenerate the starts of the evaluated segments this checkpoint covers
+        // starts of the evaluated segments this checkpoint covers
         int cnt = 0;
         if (stride == 1) {
           if (lane == 0) {
@@ -683,8 +824,7 @@ __global__ void __launch_bounds__(kThreads) render_kernel(GridP g, OptP opt, IoP
         } else {
           float tt = sm.ck_t[k], ll = sm.ck_lt[k];
           int ii = sm.ck_idx[k];
-          const int want = stride;
-          while (cnt < want) {
+          while (cnt < stride) {
             Seg s;
             march_segment(s, tt, ll, rg, g, opt, sm.links, nullptr, lane);
             if (s.evm) {
@@ -706,87 +846,99 @@ __global__ void __launch_bounds__(kThreads) render_kernel(GridP g, OptP opt, IoP
           Seg s;
           const float t0 = sm.tmp_t[b], lt0 = sm.tmp_lt[b];
           const int idx0 = sm.tmp_idx[b];
-          __syncwarp();
           march_segment(s, t0, lt0, rg, g, opt, sm.links, nullptr, lane);
           __syncwarp();
-          const float w_lane = sample_weight(s.lt_before, s.pcnt);
-          const float tn_lane = expf(s.lt_after);
-          unsigned m = s.evm;
-          int rank = __popc(m);
-          while (m) {
-            const int i = 31 - __clz(m);
-            m &= ~(1u << i);
-            --rank;
-            const int idx = idx0 + rank;
-            const int to[3] = {__shfl_sync(kFull, s.l[0], i), __shfl_sync(kFull, s.l[1], i),
-                               __shfl_sync(kFull, s.l[2], i)};
-            const float px = __shfl_sync(kFull, s.pos[0], i);
-            const float py = __shfl_sync(kFull, s.pos[1], i);
-            const float pz = __shfl_sync(kFull, s.pos[2], i);
-            const float wi = __shfl_sync(kFull, w_lane, i);
-            const float tni = __shfl_sync(kFull, tn_lane, i);
-            const float wsi = __shfl_sync(kFull, s.ws, i);
-            const float sgi = __shfl_sync(kFull, s.sigma, i);
-            if (!have_b || to[0] != bcell[0] || to[1] != bcell[1] || to[2] != bcell[2]) {
-              const int dx = to[0] - bcell[0], dy = to[1] - bcell[1], dz = to[2] - bcell[2];
+          int slot;
+          const int nR = segment_runs(s, false, 0, sm, lane, &slot);
+          const bool ev = (s.evm >> lane) & 1u;
+          const int rank = __popc(s.evm & ((1u << lane) - 1u));
+          float col[3] = {0.f, 0.f, 0.f};
+          float w8[8];
+          corner_weights(s.pos[0], s.pos[1], s.pos[2], w8);
+          if (idx0 + __popc(s.evm) <= io.cap) {
+            if (ev) {
+              col[0] = sm.col[(idx0 + rank) * 3 + 0];
+              col[1] = sm.col[(idx0 + rank) * 3 + 1];
+              col[2] = sm.col[(idx0 + rank) * 3 + 2];
+            }
+          } else {
+            // colours past the cache: gather again
+            run_colours<BD, ShT>(nR, false, sm, basis, sh, lane);
+            if (ev) lane_colour(sm, slot, w8, col);
+          }
+          // d(loss)/d(colour) pieces, trace_ray_cuvol_backward cuvol.cu:311-344
+          const float w = ev ? sample_weight(s.lt_before, s.pcnt) : 0.f;
+          const float tn = expf(s.lt_after);
+          const float sc0 = __fadd_rn(col[0], 0.5f), sc1 = __fadd_rn(col[1], 0.5f), sc2 = __fadd_rn(col[2], 0.5f);
+          const float tc = __fadd_rn(__fadd_rn(__fmul_rn(fmaxf(sc0, 0.f), gout0), __fmul_rn(fmaxf(sc2, 0.f), gout2)),
+                                     __fmul_rn(fmaxf(sc1, 0.f), gout1));
+          // light after each sample = carry + suffix sum of w * tc over the later samples
+          const float v = ev ? __fmul_rn(w, tc) : 0.f;
+          float incl = v;
+#pragma unroll
+          for (int d = 1; d < 32; d <<= 1) {
+            const float y = __shfl_down_sync(kFull, incl, d);
+            if (lane + d < 32) incl = __fadd_rn(incl, y);
+          }
+          float excl = __shfl_down_sync(kFull, incl, 1);
+          if (lane == 31) excl = 0.f;
+          const float after = __fadd_rn(carry, excl);
+          float gsig = __fmul_rn(s.ws, __fsub_rn(__fmul_rn(tc, tn), after));
+          if (io.sparsity > 0.f) {
+            const float sg = s.sigma;
+            gsig = fmaf(io.sparsity, __fdiv_rn(__fmul_rn(4.f, sg), __fadd_rn(1.f, __fmul_rn(2.f, __fmul_rn(sg, sg)))),
+                        gsig);
+          }
+          carry = __fadd_rn(carry, __shfl_sync(kFull, incl, 0));
+          const float a0 = sc0 >= 0.f ? __fmul_rn(w, gout0) : 0.f;
+          const float a1 = sc1 >= 0.f ? __fmul_rn(w, gout1) : 0.f;
+          const float a2 = sc2 >= 0.f ? __fmul_rn(w, gout2) : 0.f;
+          // accumulate per run: slot[r][g*8 + j] (g = 3: density)
+          __syncwarp();  // colours read from the slots (re-gather path) are consumed
+          for (int q = lane; q < (nR + 1) * kSlotStride; q += 32) sm.slot[q] = 0.f;
+          __syncwarp();
+          if (ev) {
+            float* d = sm.slot + slot * kSlotStride;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+              atomicAdd(d + 0 * 8 + j, __fmul_rn(w8[j], a0));
+              atomicAdd(d + 1 * 8 + j, __fmul_rn(w8[j], a1));
+              atomicAdd(d + 2 * 8 + j, __fmul_rn(w8[j], a2));
+              atomicAdd(d + 3 * 8 + j, __fmul_rn(w8[j], gsig));
+            }
+          }
+          __syncwarp();
+          // walk the runs last to first: merge shared corners, flush the others
+          for (int q = nR; q >= 1; --q) {
+            const int to0 = sm.run_l[q * 3 + 0], to1 = sm.run_l[q * 3 + 1], to2 = sm.run_l[q * 3 + 2];
+            if (!have_b || to0 != bcell[0] || to1 != bcell[1] || to2 != bcell[2]) {
+              const int dx = to0 - bcell[0], dy = to1 - bcell[1], dz = to2 - bcell[2];
               const bool near = have_b && abs(dx) <= 1 && abs(dy) <= 1 && abs(dz) <= 1;
               if (have_b) {
-                unsigned retire = 0;
-#pragma unroll
-                for (int c = 0; c < 8; ++c)
-                  if (!near || corner_src(c, -dx, -dy, -dz) < 0) retire |= 1u << c;
-                flush_corners<BD>(retire, B, lk_lane, my_basis, io.grad_sh, io.grad_density, io.mask,
-                                  lane);
+                // old corners not shared with the new cell: those on the faces -d moved across
+                const unsigned retire = near ? new_corner_mask(-dx, -dy, -dz) : 0xFFu;
+                flush_corners<BD>(retire, B, lk_lane, my_basis, io.grad_sh, io.grad_density, io.mask, lane);
+                flush_density(retire, B, lk_lane, io.grad_density, io.mask, lane);
               }
-              const int src = near ? corner_src(cj, dx, dy, dz) : -1;
-              const float moved = __shfl_sync(kFull, B, src >= 0 ? grp * 8 + src : lane);
-              B = src >= 0 ? moved : 0.f;
-              lk_lane = sm.links[i * 8 + cj];
-              bcell[0] = to[0];
-              bcell[1] = to[1];
-              bcell[2] = to[2];
+              const bool fresh = !near || ((new_corner_mask(dx, dy, dz) >> cj) & 1u);
+              const int src = fresh ? lane : grp * 8 + cj + 4 * dx + 2 * dy + dz;
+              const float moved = __shfl_sync(kFull, B, src);
+              B = fresh ? 0.f : moved;
+              lk_lane = sm.links[sm.run_lane[q] * 8 + cj];
+              bcell[0] = to0;
+              bcell[1] = to1;
+              bcell[2] = to2;
               have_b = true;
             }
-            float col;
-            if (idx < io.cap) {
-              col = grp < 3 ? sm.col[idx * 3 + grp] : 0.f;
-            } else {
-              if (!have_d || to[0] != dcell[0] || to[1] != dcell[1] || to[2] != dcell[2]) {
-                D = update_colour_corners<BD, ShT>(D, have_d, dcell, to, sm.links + i * 8, sm.tile,
-                                                   basis, sh, lane);
-                dcell[0] = to[0];
-                dcell[1] = to[1];
-                dcell[2] = to[2];
-                have_d = true;
-              }
-              col = sample_colour(D, px, py, pz, lane);
-            }
-            // d(loss)/d(colour) pieces, trace_ray_cuvol_backward cuvol.cu:311-344
-            const float sc = __fadd_rn(col, 0.5f);
-            const float part = grp < 3 ? __fmul_rn(fmaxf(sc, 0.f), gmine) : 0.f;
-            const float p0 = __shfl_sync(kFull, part, 0);
-            const float p1 = __shfl_sync(kFull, part, 8);
-            const float p2 = __shfl_sync(kFull, part, 16);
-            const float tc = __fadd_rn(__fadd_rn(p0, p2), p1);
-            float gsig = __fmul_rn(wsi, __fsub_rn(__fmul_rn(tc, tni), accum));
-            if (io.sparsity > 0.f)
-              gsig = fmaf(io.sparsity,
-                          __fdiv_rn(__fmul_rn(4.f, sgi), __fadd_rn(1.f, __fmul_rn(2.f, __fmul_rn(sgi, sgi)))),
-                          gsig);
-            accum = fmaf(wi, tc, accum);
-            const float wt = corner_weight(cj, px, py, pz);
-            if (grp < 3) {
-              const float a = (sc >= 0.f) ? __fmul_rn(wi, gmine) : 0.f;
-              B = fmaf(wt, a, B);
-            } else {
-              B = fmaf(wt, gsig, B);
-            }
+            B = __fadd_rn(B, sm.slot[q * kSlotStride + lane]);
           }
           __syncwarp();
         }
       }
-      if (have_b)
-        flush_corners<BD>(0xffu, B, lk_lane, my_basis, io.grad_sh, io.grad_density, io.mask, lane);
+      if (have_b) {
+        flush_corners<BD>(0xFFu, B, lk_lane, my_basis, io.grad_sh, io.grad_density, io.mask, lane);
+        flush_density(0xFFu, B, lk_lane, io.grad_density, io.mask, lane);
+      }
     }
     __syncwarp();
     next = __shfl_sync(kFull, next, 0);

@@ -94,6 +94,8 @@ struct IoP {
   float norm;      // 2 / (3 Q) for the fused MSE residual
   float beta;      // beta_loss / Q
   float sparsity;
+  float* accum;    // optional padded gradient rows [n_voxels][accum_stride] (SH coefficients, density, 0s)
+  int accum_stride;
   unsigned long long* work;    // ray counter (zeroed by the host)
   unsigned long long* eval_count;
   unsigned long long* trace;
@@ -252,13 +254,18 @@ __device__ __forceinline__ float skip_dist(int32_t link, const int l[3], const f
 // slots 1..32 hold this segment's runs.
 constexpr int kSlots = 33;
 constexpr int kSlotStride = 33;  // floats per slot (odd: lanes reading different slots hit different banks)
-constexpr int kTileRows = 10;    // coefficient rows gathered per pass (30 lanes = 10 rows x 3 groups)
+constexpr int kTileRows = 32;    // coefficient rows gathered per pass (one row per lane in the reduction)
 constexpr int kMaxRows = 8 * 32; // corner rows a segment can need
+constexpr int kFlushCap = 64;    // retiring corner rows listed before a flush pass
+
+__host__ __device__ constexpr int tile_floats(int C) {
+  return kTileRows * C > kFlushCap * 5 ? kTileRows * C : kFlushCap * 5;
+}
 
 struct WarpSmem {
   int* links;        // [32][8] corner links of the staged samples
   float* slot;       // [kSlots][kSlotStride]: D[j*3+g] (colour pass) or B[g*8+j] (adjoint)
-  float* tile;       // [kTileRows][C] gathered coefficient rows
+  float* tile;       // [kTileRows][C] gathered coefficient rows; in the adjoint, the flush list
   int* rowlink;      // [kMaxRows] link of each row to gather
   int* rowdst;       // [kMaxRows] slot*8 + corner of each row
   int* run_lane;     // [kSlots] first lane of each run
@@ -271,12 +278,13 @@ struct WarpSmem {
   float* tmp_t;      // [kMaxStride]
   float* tmp_lt;
   int* tmp_idx;
+  float* basis;      // [12] SH basis of the current ray
   float* col;        // [cap][3]
 };
 
 __host__ __device__ constexpr int warp_smem_floats(int C, int cap) {
-  return (32 * 8 + kSlots * kSlotStride + kTileRows * C + 2 * kMaxRows + kSlots * 6 + 3 * kNumCkpt +
-          3 * kMaxStride + 3 * cap + 3) & ~3;
+  return (32 * 8 + kSlots * kSlotStride + tile_floats(C) + 2 * kMaxRows + kSlots * 6 + 3 * kNumCkpt +
+          3 * kMaxStride + 12 + 3 * cap + 3) & ~3;
 }
 
 __device__ __forceinline__ WarpSmem carve(float* base, int C, int cap) {
@@ -284,7 +292,7 @@ __device__ __forceinline__ WarpSmem carve(float* base, int C, int cap) {
   s.links = reinterpret_cast<int*>(base);
   s.slot = base + 32 * 8;
   s.tile = s.slot + kSlots * kSlotStride;
-  s.rowlink = reinterpret_cast<int*>(s.tile + kTileRows * C);
+  s.rowlink = reinterpret_cast<int*>(s.tile + tile_floats(C));
   s.rowdst = s.rowlink + kMaxRows;
   s.run_lane = s.rowdst + kMaxRows;
   s.run_l = s.run_lane + kSlots;
@@ -296,7 +304,8 @@ __device__ __forceinline__ WarpSmem carve(float* base, int C, int cap) {
   s.tmp_t = reinterpret_cast<float*>(s.ck_idx + kNumCkpt);
   s.tmp_lt = s.tmp_t + kMaxStride;
   s.tmp_idx = reinterpret_cast<int*>(s.tmp_lt + kMaxStride);
-  s.col = reinterpret_cast<float*>(s.tmp_idx + kMaxStride);
+  s.basis = reinterpret_cast<float*>(s.tmp_idx + kMaxStride);
+  s.col = s.basis + 12;
   return s;
 }
 
@@ -347,18 +356,10 @@ __device__ __forceinline__ void march_segment(Seg& s, float t0, float lt0, const
   const long long base = (long long)s.l[0] * g.offx + (long long)s.l[1] * g.offy + s.l[2];
   s.base = base;
   const int32_t* lp = g.links + base;
-  const int32_t lk0 = valid ? __ldg(lp) : -1;
-  float skip = 0.f;
-  if (valid && lk0 < -1) skip = skip_dist(lk0, s.l, s.pos, r.d);
-  const bool is_skip = valid && skip >= opt.step;
-  const unsigned cut = __ballot_sync(kFull, !valid || is_skip);
-  s.n = cut ? __ffs(cut) - 1 : 32;
-  const bool normal = lane < s.n;
-
-  float sigma = 0.f;
-  if (normal) {
-    int lk[8];
-    lk[0] = lk0;
+  // all 8 corner links in one round trip (the cell is inside the grid for every lane)
+  int lk[8];
+  if (valid) {
+    lk[0] = __ldg(lp);
     lk[1] = __ldg(lp + 1);
     lk[2] = __ldg(lp + g.offy);
     lk[3] = __ldg(lp + g.offy + 1);
@@ -366,6 +367,19 @@ __device__ __forceinline__ void march_segment(Seg& s, float t0, float lt0, const
     lk[5] = __ldg(lp + g.offx + 1);
     lk[6] = __ldg(lp + g.offx + g.offy);
     lk[7] = __ldg(lp + g.offx + g.offy + 1);
+  } else {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) lk[j] = -1;
+  }
+  float skip = 0.f;
+  if (valid && lk[0] < -1) skip = skip_dist(lk[0], s.l, s.pos, r.d);
+  const bool is_skip = valid && skip >= opt.step;
+  const unsigned cut = __ballot_sync(kFull, !valid || is_skip);
+  s.n = cut ? __ffs(cut) - 1 : 32;
+  const bool normal = lane < s.n;
+
+  float sigma = 0.f;
+  if (normal) {
     float v[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) v[j] = lk[j] >= 0 ? __ldg(g.density + lk[j]) : 0.f;
@@ -563,22 +577,33 @@ __device__ __forceinline__ void run_colours(int nR, bool have_prev, const WarpSm
     }
   }
   __syncwarp();
-  // gather and reduce, kTileRows rows per pass
-  const int rr = lane / 3, gg = lane - 3 * (lane / 3);
+  // gather and reduce, kTileRows rows per pass: loads are issued 8 rows at a time
+  // so that a pass costs one memory round trip
   for (int m0 = 0; m0 < M; m0 += kTileRows) {
     const int nrow = min(kTileRows, M - m0);
-    for (int q = 0; q < nrow; ++q) {
-      const int lk = sm.rowlink[m0 + q];
-      if (lane < C) sm.tile[q * C + lane] = lk >= 0 ? ldg_f32(sh + (long long)lk * C + lane) : 0.f;
+    for (int q0 = 0; q0 < nrow; q0 += 8) {
+      float x[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int lk = (q0 + u < nrow) ? sm.rowlink[m0 + q0 + u] : -1;
+        x[u] = (lane < C && lk >= 0) ? ldg_f32(sh + (long long)lk * C + lane) : 0.f;
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        if (q0 + u < nrow && lane < C) sm.tile[(q0 + u) * C + lane] = x[u];
     }
     __syncwarp();
-    if (rr < nrow) {
-      const float* row = sm.tile + rr * C + gg * BD;
-      float acc = 0.f;
+    if (lane < nrow) {
+      const float* row = sm.tile + lane * C;
+      const int dst = sm.rowdst[m0 + lane];
+      float* out = sm.slot + (dst >> 3) * kSlotStride + (dst & 7) * 3;
 #pragma unroll
-      for (int k = 0; k < BD; ++k) acc = fmaf(basis[k], row[k], acc);
-      const int dst = sm.rowdst[m0 + rr];
-      sm.slot[(dst >> 3) * kSlotStride + (dst & 7) * 3 + gg] = acc;
+      for (int gg = 0; gg < 3; ++gg) {
+        float acc = 0.f;
+#pragma unroll
+        for (int k = 0; k < BD; ++k) acc = fmaf(basis[k], row[gg * BD + k], acc);
+        out[gg] = acc;
+      }
     }
     __syncwarp();
   }
@@ -609,31 +634,76 @@ __device__ __forceinline__ void lane_colour(const WarpSmem& sm, int slot, const 
   col[2] = c2;
 }
 
-// Flush the gradient accumulators of the retiring corners of the tracked cell.
-// Lane L holds B for (group L>>3, corner L&7); group 3 is the density.
-template <int BD>
-__device__ __forceinline__ void flush_corners(unsigned retire, float B, int lk_lane, float my_basis,
-                                              float* __restrict__ grad_sh, float* __restrict__ grad_density,
-                                              uint8_t* __restrict__ mask, int lane) {
-  constexpr int C = 3 * BD;
-  const int src_group = lane < C ? lane / BD : 0;
-  while (retire) {
-    const int c = __ffs(retire) - 1;
-    retire &= retire - 1;
-    const int lk = __shfl_sync(kFull, lk_lane, c);
-    const float b = __shfl_sync(kFull, B, src_group * 8 + c);
-    if (lk >= 0 && lane < C && b != 0.f && grad_sh != nullptr)
-      atomicAdd(grad_sh + (long long)lk * C + lane, __fmul_rn(my_basis, b));
+// The adjoint lists retiring corners (their 4 accumulators and link) in shared
+// memory and flushes the list in one pass: per corner row, lanes 0..C-1 add
+// basis_k * B[group] to the row's C coefficients (one coalesced atomic add) and
+// lane C adds the density gradient and marks the voxel.  Lane L holds B for
+// (group L>>3, corner L&7); group 3 is the density.
+__device__ __forceinline__ void list_retiring(unsigned retire, float B, int lk_lane, float* fl_val,
+                                              int* fl_link, int F, int lane) {
+  const int j = lane & 7, grp = lane >> 3;
+  if ((retire >> j) & 1u) {
+    const int o = F + __popc(retire & ((1u << j) - 1u));
+    fl_val[o * 4 + grp] = B;
+    if (grp == 0) fl_link[o] = lk_lane;
   }
 }
 
-__device__ __forceinline__ void flush_density(unsigned retire, float B, int lk_lane,
-                                              float* __restrict__ grad_density, uint8_t* __restrict__ mask,
-                                              int lane) {
-  if (lane >= 24 && ((retire >> (lane - 24)) & 1u) && lk_lane >= 0) {
-    if (grad_density != nullptr && B != 0.f) atomicAdd(grad_density + lk_lane, B);
-    if (mask != nullptr) mask[lk_lane] = 1;
+// Vector flush into the padded rows: lane q adds channels 4q..4q+3 of a padded row
+// (SH coefficients 0..C-1, the density at C, then zeros) with one float4 atomic add,
+// ceil((C+1)/4) operations per corner row instead of C+1 scalar ones (the L2's
+// atomic throughput is counted in operations).  basis: the ray's SH basis in
+// shared memory.
+template <int BD>
+__device__ __forceinline__ void flush_list_vec(int F, const float* fl_val, const int* fl_link, const float* basis,
+                                               float* __restrict__ accum, int stride, uint8_t* __restrict__ mask,
+                                               int lane) {
+  constexpr int C = 3 * BD;
+  __syncwarp();
+  const int nvec = stride >> 2;
+  float coef[4];
+  int grp[4];
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    const int c = 4 * lane + e;
+    coef[e] = c < C ? basis[c % BD] : 1.f;
+    grp[e] = c < C ? c / BD : (c == C ? 3 : 4);
   }
+  for (int f = 0; f < F; ++f) {
+    const int lk = fl_link[f];
+    if (lk < 0) continue;
+    if (lane < nvec) {
+      float x[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) x[e] = grp[e] < 4 ? __fmul_rn(coef[e], fl_val[f * 4 + grp[e]]) : 0.f;
+      if (x[0] != 0.f || x[1] != 0.f || x[2] != 0.f || x[3] != 0.f)
+        atomicAdd(reinterpret_cast<float4*>(accum + (long long)lk * stride) + lane, make_float4(x[0], x[1], x[2], x[3]));
+    } else if (lane == 31 && mask != nullptr) {
+      mask[lk] = 1;
+    }
+  }
+  __syncwarp();
+}
+
+template <int BD>
+__device__ __forceinline__ void flush_list(int F, const float* fl_val, const int* fl_link, float my_basis,
+                                           float* __restrict__ grad_sh, float* __restrict__ grad_density,
+                                           uint8_t* __restrict__ mask, int lane) {
+  constexpr int C = 3 * BD;
+  __syncwarp();
+  const int gsel = lane < C ? lane / BD : 3;
+  for (int f = 0; f < F; ++f) {
+    const int lk = fl_link[f];
+    if (lk < 0) continue;
+    const float b = fl_val[f * 4 + gsel];
+    if (lane < C) {
+      if (b != 0.f && grad_sh != nullptr) atomicAdd(grad_sh + (long long)lk * C + lane, __fmul_rn(my_basis, b));
+    } else if (lane == C) {
+      if (b != 0.f && grad_density != nullptr) atomicAdd(grad_density + lk, b);
+      if (mask != nullptr) mask[lk] = 1;
+    }
+  }
+  __syncwarp();
 }
 
 // ---------------------------------------------------------------- kernel
@@ -674,6 +744,9 @@ __global__ void __launch_bounds__(kThreads) render_kernel(GridP g, OptP opt, IoP
 #pragma unroll
     for (int k = 0; k < BD; ++k)
       if (lane % BD == k) my_basis = basis[k];
+#pragma unroll
+    for (int k = 0; k < BD; ++k)
+      if (lane == k) sm.basis[k] = basis[k];
     RayGeo rg;
     find_bounds(rg, org, dir, g, opt);
     unsigned long long th = 1469598103934665603ull;
@@ -908,7 +981,10 @@ __global__ void __launch_bounds__(kThreads) render_kernel(GridP g, OptP opt, IoP
             }
           }
           __syncwarp();
-          // walk the runs last to first: merge shared corners, flush the others
+          // walk the runs last to first: merge shared corners, list the others, flush the list
+          float* fl_val = sm.tile;
+          int* fl_link = reinterpret_cast<int*>(sm.tile + kFlushCap * 4);
+          int F = 0;
           for (int q = nR; q >= 1; --q) {
             const int to0 = sm.run_l[q * 3 + 0], to1 = sm.run_l[q * 3 + 1], to2 = sm.run_l[q * 3 + 2];
             if (!have_b || to0 != bcell[0] || to1 != bcell[1] || to2 != bcell[2]) {
@@ -917,8 +993,15 @@ __global__ void __launch_bounds__(kThreads) render_kernel(GridP g, OptP opt, IoP
               if (have_b) {
                 // old corners not shared with the new cell: those on the faces -d moved across
                 const unsigned retire = near ? new_corner_mask(-dx, -dy, -dz) : 0xFFu;
-                flush_corners<BD>(retire, B, lk_lane, my_basis, io.grad_sh, io.grad_density, io.mask, lane);
-                flush_density(retire, B, lk_lane, io.grad_density, io.mask, lane);
+                if (F + 8 > kFlushCap) {
+                  if (io.accum != nullptr)
+                    flush_list_vec<BD>(F, fl_val, fl_link, sm.basis, io.accum, io.accum_stride, io.mask, lane);
+                  else
+                    flush_list<BD>(F, fl_val, fl_link, my_basis, io.grad_sh, io.grad_density, io.mask, lane);
+                  F = 0;
+                }
+                list_retiring(retire, B, lk_lane, fl_val, fl_link, F, lane);
+                F += __popc(retire);
               }
               const bool fresh = !near || ((new_corner_mask(dx, dy, dz) >> cj) & 1u);
               const int src = fresh ? lane : grp * 8 + cj + 4 * dx + 2 * dy + dz;
@@ -932,12 +1015,20 @@ __global__ void __launch_bounds__(kThreads) render_kernel(GridP g, OptP opt, IoP
             }
             B = __fadd_rn(B, sm.slot[q * kSlotStride + lane]);
           }
-          __syncwarp();
+          if (io.accum != nullptr)
+            flush_list_vec<BD>(F, fl_val, fl_link, sm.basis, io.accum, io.accum_stride, io.mask, lane);
+          else
+            flush_list<BD>(F, fl_val, fl_link, my_basis, io.grad_sh, io.grad_density, io.mask, lane);
         }
       }
       if (have_b) {
-        flush_corners<BD>(0xFFu, B, lk_lane, my_basis, io.grad_sh, io.grad_density, io.mask, lane);
-        flush_density(0xFFu, B, lk_lane, io.grad_density, io.mask, lane);
+        float* fl_val = sm.tile;
+        int* fl_link = reinterpret_cast<int*>(sm.tile + kFlushCap * 4);
+        list_retiring(0xFFu, B, lk_lane, fl_val, fl_link, 0, lane);
+        if (io.accum != nullptr)
+          flush_list_vec<BD>(8, fl_val, fl_link, sm.basis, io.accum, io.accum_stride, io.mask, lane);
+        else
+          flush_list<BD>(8, fl_val, fl_link, my_basis, io.grad_sh, io.grad_density, io.mask, lane);
       }
     }
     __syncwarp();
@@ -947,6 +1038,22 @@ __global__ void __launch_bounds__(kThreads) render_kernel(GridP g, OptP opt, IoP
 }
 
 // ---------------------------------------------------------------- host side
+
+// grad_sh[v, c] += accum[v, c], grad_density[v] += accum[v, C] for rows with any
+// non-zero entry (untouched rows keep their exact values).
+__global__ void __launch_bounds__(256) add_accum_kernel(const float* __restrict__ accum, int stride, int C,
+                                                        long long n, float* __restrict__ grad_sh,
+                                                        float* __restrict__ grad_density) {
+  const int lane = threadIdx.x & 31;
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long v = warp; v < n; v += nwarps) {
+    const float x = lane < stride ? accum[v * stride + lane] : 0.f;
+    if (__ballot_sync(0xffffffffu, x != 0.f) == 0u) continue;
+    if (lane < C && grad_sh != nullptr) grad_sh[v * C + lane] += x;
+    if (lane == C && grad_density != nullptr) grad_density[v] += x;
+  }
+}
 
 int g_cap = kDefaultCap;
 
@@ -1063,17 +1170,34 @@ static int make_opt(const svx_render_opts_t* o, OptP* p) {
   return SVX_OK;
 }
 
-// Scratch: the ray counter.  Stream-ordered allocation, released after the launch.
+// Per-call scratch: stream-ordered allocations released after the launches.  The
+// device's default memory pool keeps freed blocks (release threshold raised once per
+// device), so steady-state calls do not go back to the driver.
 struct Scratch {
-  unsigned long long* p = nullptr;
+  void* p[2] = {nullptr, nullptr};
   cudaStream_t st;
   explicit Scratch(cudaStream_t s) : st(s) {}
-  int alloc() {
-    SVX_CUDA_TRY(cudaMallocAsync((void**)&p, 256, st));
+  int alloc(int i, size_t bytes) {
+    static std::mutex mu;
+    static bool tuned[64] = {false};
+    int dev = 0;
+    SVX_CUDA_TRY(cudaGetDevice(&dev));
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      if (dev >= 0 && dev < 64 && !tuned[dev]) {
+        cudaMemPool_t pool;
+        SVX_CUDA_TRY(cudaDeviceGetDefaultMemPool(&pool, dev));
+        uint64_t thr = ~0ull;
+        SVX_CUDA_TRY(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+        tuned[dev] = true;
+      }
+    }
+    SVX_CUDA_TRY(cudaMallocAsync(&p[i], bytes, st));
     return SVX_OK;
   }
   ~Scratch() {
-    if (p) cudaFreeAsync(p, st);
+    for (void* q : p)
+      if (q) cudaFreeAsync(q, st);
   }
 };
 
@@ -1108,10 +1232,32 @@ static int render_rays(const svx_grid_t* grid, const svx_rays_t* rays, const svx
   io.cap = g_cap;
   cudaStream_t st = as_stream(stream);
   Scratch scr(st);
-  rc = scr.alloc();
+  rc = scr.alloc(0, 256);
   if (rc) return rc;
-  io.work = scr.p;
-  return dispatch<MODE, false>(grid, g, o, io, rays->n_rays, st);
+  io.work = reinterpret_cast<unsigned long long*>(scr.p[0]);
+  const bool grads = MODE != kFwd && (io.grad_sh != nullptr || io.grad_density != nullptr);
+  const int C = grid->sh_data_dim;
+  const int stride = (C + 1 + 3) & ~3;
+  if (grads) {
+    // gradient rows padded to 16 bytes, accumulated with vector atomics, then added once
+    const size_t bytes = sizeof(float) * (size_t)stride * (size_t)grid->n_voxels;
+    rc = scr.alloc(1, bytes > 0 ? bytes : 16);
+    if (rc) return rc;
+    SVX_CUDA_TRY(cudaMemsetAsync(scr.p[1], 0, bytes, st));
+    io.accum = reinterpret_cast<float*>(scr.p[1]);
+    io.accum_stride = stride;
+  }
+  rc = dispatch<MODE, false>(grid, g, o, io, rays->n_rays, st);
+  if (rc) return rc;
+  if (grads && grid->n_voxels > 0) {
+    long long blocks = (grid->n_voxels + 7) / 8;
+    const long long cap = (long long)num_sms() * 32;
+    if (blocks > cap) blocks = cap;
+    add_accum_kernel<<<(unsigned)blocks, 256, 0, st>>>(io.accum, stride, C, grid->n_voxels, io.grad_sh,
+                                                       io.grad_density);
+    SVX_LAUNCH_CHECK("add_accum_kernel");
+  }
+  return SVX_OK;
 }
 
 }  // namespace svx
@@ -1195,9 +1341,9 @@ extern "C" int svx_volume_render_cuvol_image(const svx_grid_t* grid, const svx_c
   io.cap = 0;
   cudaStream_t st = as_stream(stream);
   Scratch scr(st);
-  rc = scr.alloc();
+  rc = scr.alloc(0, 256);
   if (rc) return rc;
-  io.work = scr.p;
+  io.work = reinterpret_cast<unsigned long long*>(scr.p[0]);
   return dispatch<kFwd, true>(grid, g, o, io, n, st);
 }
 

@@ -33,6 +33,8 @@
 //     the ray leaves it (the reference issues 8 x 27 atomics per sample).
 #include "common.cuh"
 
+#include <cub/cub.cuh>
+
 #include <climits>
 #include <cmath>
 #include <mutex>
@@ -46,6 +48,7 @@ constexpr int kWarps = kThreads / 32;
 constexpr int kNumCkpt = 64;   // stored segment checkpoints per ray before thinning
 constexpr int kMaxStride = 64; // checkpoint thinning limit: 64*64 segments per ray
 constexpr int kDefaultCap = 192;
+constexpr long long kSortMinRays = 1 << 15;  // batches below this run in input order
 
 enum Mode { kFwd = 0, kFused = 1, kBwd = 2 };
 
@@ -96,6 +99,7 @@ struct IoP {
   float sparsity;
   float* accum;    // optional padded gradient rows [n_voxels][accum_stride] (SH coefficients, density, 0s)
   int accum_stride;
+  const int* order;            // optional processing order of the rays (a permutation)
   unsigned long long* work;    // ray counter (zeroed by the host)
   unsigned long long* eval_count;
   unsigned long long* trace;
@@ -725,7 +729,7 @@ __global__ void __launch_bounds__(kThreads) render_kernel(GridP g, OptP opt, IoP
   next = __shfl_sync(kFull, next, 0);
 
   while (next < (unsigned long long)io.n_rays) {
-    const long long ray = (long long)next;
+    const long long ray = io.order != nullptr ? (long long)__ldg(io.order + next) : (long long)next;
     if (lane == 0) next = atomicAdd(io.work, 1ull);  // prefetch the following ray
     // ---- ray setup (all lanes, redundantly)
     float org[3], dir[3];
@@ -1037,6 +1041,58 @@ __global__ void __launch_bounds__(kThreads) render_kernel(GridP g, OptP opt, IoP
   if (io.eval_count != nullptr && lane == 0 && evals) atomicAdd(io.eval_count, evals);
 }
 
+// ---------------------------------------------------------------- ray order
+
+// Coherence key of a ray: 4 bits of direction (2 x 2 bits of its octahedral map)
+// above the 24-bit Morton code of the midpoint of its chord through the grid.
+// Rays with equal keys run nearly parallel through the same region, so warps that
+// run them at the same time share cached corner rows and gradient lines.  Rays
+// that miss the grid sort last.
+__device__ __forceinline__ unsigned spread_bits3(unsigned v) {
+  v &= 0xFFu;
+  v = (v | (v << 8)) & 0x0300F00Fu;
+  v = (v | (v << 4)) & 0x030C30C3u;
+  v = (v | (v << 2)) & 0x09249249u;
+  return v;
+}
+
+__global__ void __launch_bounds__(256) ray_keys_kernel(GridP g, OptP opt, const float* __restrict__ origins,
+                                                       const float* __restrict__ dirs, long long n,
+                                                       unsigned* __restrict__ keys, int* __restrict__ vals) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    float org[3], dir[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      org[j] = __ldg(origins + i * 3 + j);
+      dir[j] = __ldg(dirs + i * 3 + j);
+    }
+    RayGeo r;
+    find_bounds(r, org, dir, g, opt);
+    unsigned key = 0xFFFFFFFFu;
+    if (r.tmin <= r.tmax) {
+      const float tm = 0.5f * (r.tmin + r.tmax);
+      unsigned m = 0;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const float p = fminf(fmaxf(fmaf(tm, r.d[j], r.o[j]) / (float)g.size[j], 0.f), 0.999f);
+        m |= spread_bits3((unsigned)(p * 256.f)) << (2 - j);
+      }
+      const float s = fabsf(r.d[0]) + fabsf(r.d[1]) + fabsf(r.d[2]);
+      float u = r.d[0] / s, v = r.d[1] / s;
+      if (r.d[2] < 0.f) {
+        const float uu = (1.f - fabsf(v)) * (u >= 0.f ? 1.f : -1.f);
+        v = (1.f - fabsf(u)) * (v >= 0.f ? 1.f : -1.f);
+        u = uu;
+      }
+      const unsigned qu = min((unsigned)((u + 1.f) * 2.f), 3u), qv = min((unsigned)((v + 1.f) * 2.f), 3u);
+      key = ((qu << 2 | qv) << 24) | m;
+    }
+    keys[i] = key;
+    vals[i] = (int)i;
+  }
+}
+
 // ---------------------------------------------------------------- host side
 
 // grad_sh[v, c] += accum[v, c], grad_density[v] += accum[v, C] for rows with any
@@ -1174,7 +1230,7 @@ static int make_opt(const svx_render_opts_t* o, OptP* p) {
 // device's default memory pool keeps freed blocks (release threshold raised once per
 // device), so steady-state calls do not go back to the driver.
 struct Scratch {
-  void* p[2] = {nullptr, nullptr};
+  void* p[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaStream_t st;
   explicit Scratch(cudaStream_t s) : st(s) {}
   int alloc(int i, size_t bytes) {
@@ -1246,6 +1302,29 @@ static int render_rays(const svx_grid_t* grid, const svx_rays_t* rays, const svx
     SVX_CUDA_TRY(cudaMemsetAsync(scr.p[1], 0, bytes, st));
     io.accum = reinterpret_cast<float*>(scr.p[1]);
     io.accum_stride = stride;
+  }
+  if (rays->n_rays >= kSortMinRays && rays->n_rays < (1ll << 31)) {
+    // process the rays in coherence-key order
+    const long long n = rays->n_rays;
+    size_t tmp_bytes = 0;
+    SVX_CUDA_TRY(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, (const unsigned*)nullptr, (unsigned*)nullptr,
+                                                 (const int*)nullptr, (int*)nullptr, (int)n, 0, 32, st));
+    const size_t off_keys2 = ((size_t)n * 4 + 255) & ~(size_t)255;
+    const size_t off_vals = 2 * off_keys2, off_vals2 = 3 * off_keys2, off_tmp = 4 * off_keys2;
+    rc = scr.alloc(2, off_tmp + tmp_bytes);
+    if (rc) return rc;
+    char* base = reinterpret_cast<char*>(scr.p[2]);
+    unsigned* k_in = reinterpret_cast<unsigned*>(base);
+    unsigned* k_out = reinterpret_cast<unsigned*>(base + off_keys2);
+    int* v_in = reinterpret_cast<int*>(base + off_vals);
+    int* v_out = reinterpret_cast<int*>(base + off_vals2);
+    long long blocks = (n + 255) / 256;
+    if (blocks > (long long)num_sms() * 16) blocks = (long long)num_sms() * 16;
+    ray_keys_kernel<<<(unsigned)blocks, 256, 0, st>>>(g, o, rays->origins, rays->dirs, n, k_in, v_in);
+    SVX_LAUNCH_CHECK("ray_keys_kernel");
+    SVX_CUDA_TRY(cub::DeviceRadixSort::SortPairs(base + off_tmp, tmp_bytes, k_in, k_out, v_in, v_out, (int)n, 0, 32,
+                                                 st));
+    io.order = v_out;
   }
   rc = dispatch<MODE, false>(grid, g, o, io, rays->n_rays, st);
   if (rc) return rc;

@@ -116,6 +116,16 @@ def test_fused_last_sample_opaque():
     _run_fused(spec, og, rays_pair(o, d), o, d, gt, opt, oopt, grad_ref="f64")
 
 
+def test_fused_sorted_batch():
+    """Batches of 32768 rays and more run in coherence-key order (a permutation
+    applied inside the library); results land at the rays' own positions."""
+    g = S.make_grid(48, occupancy=0.3, seed=61)
+    spec, og = grid_pair(g)
+    o, d, gt = S.make_rays(40000, seed=62)
+    opt, oopt = opt_struct()
+    _run_fused(spec, og, rays_pair(o, d), o, d, gt, opt, oopt, check_f64=False)
+
+
 def test_fused_beta_sparsity():
     g = S.make_grid(32, occupancy=0.3, seed=5)
     spec, og = grid_pair(g)

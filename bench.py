@@ -247,6 +247,166 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def run_mixed(args):
+    """Mixed-precision configuration: 512^3 grid, 8% occupancy (32 balls), SH stored
+    as bfloat16 or float16 (density float32, all arithmetic float32) against the
+    float32 form: PSNR of an 800x800 render from a fixed camera, relative error of
+    the fused-step gradients over 4M rays, and fused-step throughput."""
+    from svox2_gb300 import Camera, Rays, SparseGrid
+    from svox2_gb300 import synthetic as S
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    reso, occ, n_balls, q = 512, 0.08, 32, 4_000_000
+    g = S.make_grid(reso, occupancy=occ, n_balls=n_balls, seed=0, device=dev)
+    o, d, gt = [t.to(dev) for t in S.make_rays(q, seed=2000)]
+    c2w = S.look_at_c2w((0.0, 0.0, -4.0)).to(dev)
+    cam = Camera(c2w, fx=1111.0, fy=1111.0, cx=400.0, cy=400.0, width=800, height=800)
+    res = {}
+    ref_img = ref_gd = ref_gs = None
+    for name, dt in (("fp32", torch.float32), ("bf16", torch.bfloat16), ("fp16", torch.float16)):
+        grid = SparseGrid.from_tables(g.links.to(dev), g.density.to(dev), g.sh.to(dev).to(dt))
+        grid.opt.sigma_thresh, grid.opt.stop_thresh = 1e-8, 1e-7
+        with torch.no_grad():
+            img = grid.volume_render_image(cam)
+        rays = Rays(o, d)
+        grid.volume_render_fused(rays, gt)          # gradients of one step (from zero)
+        gd, gs = [t.clone() for t in grid._get_data_grads()]
+        # throughput: fused render + TV + RMSprop, as the training step
+        for _ in range(2):
+            train_step(grid, o, d, gt)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            train_step(grid, o, d, gt)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        entry = {"rays_per_s": q / (ms / 1e3), "ms_per_step": ms,
+                 "sh_bytes": int(grid.sh_data.numel() * grid.sh_data.element_size())}
+        if ref_img is None:
+            ref_img, ref_gd, ref_gs = img, gd, gs
+        else:
+            mse = float(torch.mean((img - ref_img) ** 2))
+            entry["psnr_vs_fp32_db"] = float("inf") if mse == 0 else -10.0 * np.log10(mse)
+            entry["grad_density_rel_err"] = float(torch.norm(gd - ref_gd) / torch.norm(ref_gd))
+            entry["grad_sh_rel_err"] = float(torch.norm(gs - ref_gs) / torch.norm(ref_gs))
+        res[name] = entry
+        del grid
+        torch.cuda.empty_cache()
+    line = {"metric": "mixed-precision SH storage at 512^3 8% occupancy: render PSNR and gradient error vs FP32, "
+                      "train-step rays/s", "unit": "rays/s", "steps": args.steps, "data": "synthetic",
+            "config": {"workload": "512^3, 32 balls, 8% occupancy, SH9; 4M rays/step; 800x800 image fx=fy=1111 "
+                                   "from (0,0,-4)", "n_voxels": int(g.density.shape[0]),
+                       "occupancy": float(g.occupancy)}, "results": res}
+    print(json.dumps(line), flush=True)
+
+
+def run_serve(args):
+    """Serving configuration: a Poisson stream (2000 requests/s) of render requests (square
+    images, side U{64..800}, cameras on a radius-4 sphere looking at the origin) and train-step
+    requests (rays ~ logU[4096, 262144]) against 16 resident grids (128^3..256^3, 5-25%
+    occupancy, BF16 SH) admitted under a 150 GB budget.  The same stream runs through the
+    continuous-batching RenderServer and through serial plain launches (one request at a
+    time, the plain grid API), each from identical initial grids; reported are throughput
+    and p50/p99 latency (arrival to result on the host) of both."""
+    from svox2_gb300 import Camera, Rays, SparseGrid
+    from svox2_gb300 import synthetic as S
+    from svox2_gb300.serving import RenderRequest, RenderServer, TrainRequest, latency_stats
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    rng = np.random.default_rng(7)
+    n_req = args.requests
+    datas = {}
+    for i in range(16):
+        reso = int(rng.integers(128, 257))
+        occ = float(rng.uniform(0.05, 0.25))
+        datas[f"g{i}"] = S.make_grid(reso, occupancy=occ, n_balls=8, seed=100 + i, device=dev)
+
+    def fresh(g):
+        grid = SparseGrid.from_tables(g.links.to(dev), g.density.to(dev), g.sh.to(dev).to(torch.bfloat16))
+        grid.opt.sigma_thresh, grid.opt.stop_thresh = 1e-8, 1e-7
+        return grid
+
+    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, size=n_req))
+    reqs = []
+    for i in range(n_req):
+        gid = f"g{int(rng.integers(16))}"
+        if rng.random() < 0.5:
+            side = int(rng.integers(64, 801))
+            v = rng.normal(size=3)
+            eye = 4.0 * v / np.linalg.norm(v)
+            reqs.append(RenderRequest(gid, S.look_at_c2w(tuple(eye)), side, side, fx=1.389 * side))
+        else:
+            q = int(np.exp(rng.uniform(np.log(4096), np.log(262144))))
+            o, d, gt = S.make_rays(q, seed=5000 + i)
+            reqs.append(TrainRequest(gid, o.pin_memory(), d.pin_memory(), gt.pin_memory(), tv_seed=i))
+    total_rays = sum(r.width * r.height if isinstance(r, RenderRequest) else r.origins.shape[0] for r in reqs)
+
+    # ---- continuous batching
+    server = RenderServer(device=dev, hbm_budget=150e9, batch_rays=1 << 20, chunk_rays=1 << 18)
+    for k, g in datas.items():
+        server.add_grid(k, fresh(g), trainable=True)
+    # warm-up: one request of each kind (graphs captured, kernels loaded), not timed
+    warm = [server.submit(RenderRequest("g0", S.look_at_c2w((0.0, 0.0, -4.0)), 64, 64, fx=90.0)),
+            server.submit(TrainRequest("g0", *S.make_rays(4096, seed=1), tv_seed=0))]
+    server.run_until_idle()
+    for k, g in datas.items():          # back to the initial grids
+        server.remove_grid(k)
+        server.add_grid(k, fresh(g), trainable=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    tickets = []
+    i = 0
+    while i < n_req or not server.idle():
+        now = time.perf_counter() - t0
+        while i < n_req and arrivals[i] <= now:
+            tickets.append(server.submit(reqs[i], now=t0 + arrivals[i]))
+            i += 1
+        server.step()
+    span_b = time.perf_counter() - t0
+    stats_b = latency_stats(tickets)
+
+    # ---- serial plain launches
+    grids = {k: fresh(g) for k, g in datas.items()}
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    lat = []
+    for r, a in zip(reqs, arrivals):
+        now = time.perf_counter() - t0
+        if now < a:
+            time.sleep(a - now)
+        grid = grids[r.grid_id]
+        if isinstance(r, RenderRequest):
+            with torch.no_grad():
+                grid.volume_render_image(Camera(r.c2w.to(dev), fx=r.fx, width=r.width, height=r.height)).cpu()
+        else:
+            rgb = grid.volume_render_fused(Rays(r.origins.to(dev), r.dirs.to(dev)), r.rgb_gt.to(dev))
+            np.random.seed(r.tv_seed)
+            grid.inplace_tv_grad(grid._grad_buffer(grid.density_data), scaling=r.tv_density, sparse_frac=r.tv_frac)
+            grid.inplace_tv_color_grad(grid._grad_buffer(grid.sh_data), scaling=r.tv_sh, sparse_frac=r.tv_frac)
+            grid.optim_density_step(r.lr_density, beta=r.rms_beta)
+            grid.optim_sh_step(r.lr_sh, beta=r.rms_beta)
+            rgb.cpu()
+        lat.append(time.perf_counter() - t0 - a)
+    span_s = time.perf_counter() - t0
+    lat = np.array(lat)
+    stats_s = {"n": int(lat.size), "p50_ms": float(np.percentile(lat, 50) * 1e3),
+               "p99_ms": float(np.percentile(lat, 99) * 1e3), "mean_ms": float(lat.mean() * 1e3)}
+    line = {"metric": "serving: requests/s and p50/p99 latency, continuous batching vs serial plain launches",
+            "unit": "requests/s", "value": n_req / span_b, "data": "synthetic",
+            "config": {"workload": "Poisson %.0f req/s, %d requests, 50%% renders (side U{64..800}) / 50%% train "
+                                   "steps (logU[4096, 262144] rays), 16 grids 128^3..256^3 5-25%% occupancy BF16 SH, "
+                                   "150 GB budget" % (args.rate, n_req), "total_rays": int(total_rays)},
+            "batched": {"requests_per_s": n_req / span_b, "rays_per_s": total_rays / span_b, "makespan_s": span_b,
+                        **stats_b, "batches": server.batches},
+            "serial": {"requests_per_s": n_req / span_s, "rays_per_s": total_rays / span_s, "makespan_s": span_s,
+                       **stats_s}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     global Q
     ap = argparse.ArgumentParser()
@@ -257,7 +417,18 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--rays", type=int, default=1_000_000, help="rays per step (profiling runs use a smaller case)")
     ap.add_argument("--skip-e2e", action="store_true", help="leave out the host-copy arm (profiling runs)")
+    ap.add_argument("--config", default="train", choices=["train", "mixed", "serve"],
+                    help="train: the 256^3 training step (default); mixed: 512^3 BF16/FP16 SH vs FP32; "
+                         "serve: continuous-batching server vs serial launches")
+    ap.add_argument("--requests", type=int, default=600, help="serve: number of requests in the stream")
+    ap.add_argument("--rate", type=float, default=2000.0, help="serve: Poisson arrival rate (requests/s)")
     args = ap.parse_args()
+    if args.config == "mixed":
+        run_mixed(args)
+        return
+    if args.config == "serve":
+        run_serve(args)
+        return
     Q = args.rays
     args.warmup = max(args.warmup, 3)
 

@@ -174,6 +174,46 @@ int svx_volume_render_cuvol_fused_noalloc(const svx_grid_t* grid, const svx_rays
                                           const svx_grid_grads_t* grads,
                                           const svx_render_stats_t* stats, void* stream);
 
+/* ---- serving: batched launches over several resident grids -------------
+ * No counterpart in the reference (it renders one grid per call).  A serving
+ * loop puts the rays of several requests, on several resident grids, into one
+ * persistent launch.  All grids of a batch share basis_dim and sh_dtype. */
+
+/* One grid of a batch, read by the kernel from DEVICE memory.  For the fused
+ * mode: where this grid's gradients go (accum: optional padded rows
+ * [n_voxels][accum_stride], accum_stride a multiple of 4 >= sh_data_dim + 1,
+ * zeroed by the caller, added into the gradients by the caller), and the MSE
+ * scale norm = 2 / (3 * rays of this grid's request) with the beta / sparsity
+ * loss weights (beta already divided by that ray count). */
+typedef struct {
+  svx_grid_t grid;
+  svx_grid_grads_t grads;
+  float* accum;
+  int32_t accum_stride;
+  float norm;
+  float beta;
+  float sparsity;
+} svx_batch_grid_t;
+
+/* Render (mode 0) or fused-MSE render (mode 1) of a batch of rays.
+ *   grids       device array of svx_batch_grid_t; the host does not read it,
+ *               so the caller vouches for it (pointers, sizes, basis_dim)
+ *   ray_grid    device int32 [max_rays], the grid of each ray
+ *   n_rays_dev  device int64: rays processed by this launch (<= max_rays); it
+ *               is read on the device, so that a captured CUDA graph of this
+ *               call can be replayed for a new batch after the buffers change
+ *   work        device uint64 scratch of the caller (cleared by the call)
+ * Allocates nothing.  max_rays sizes the persistent grid. */
+int svx_render_batch(int32_t mode, const svx_batch_grid_t* grids, int32_t basis_dim, int32_t sh_dtype,
+                     const float* origins, const float* dirs, const int32_t* ray_grid,
+                     const int64_t* n_rays_dev, int64_t max_rays, const svx_render_opts_t* opt,
+                     const float* rgb_gt, float* rgb_out, uint64_t* work, void* stream);
+
+/* The rays of a pinhole camera (what volume_render_cuvol_image marches,
+ * cam2world_ray in svox2/csrc/include/render_util.cuh:526-544), written as
+ * origins / dirs float32 [height * width, 3] in row-major pixel order. */
+int svx_camera_rays(const svx_camera_t* cam, float* origins, float* dirs, void* stream);
+
 /* ---- point sampling: svox2/csrc/svox2_kernel.cu ------------------------ */
 
 /* sample_grid (svox2/csrc/svox2.cpp:11-12, svox2_kernel.cu:181-217).

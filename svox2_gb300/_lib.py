@@ -82,6 +82,11 @@ class SvxRenderStats(C.Structure):
     _fields_ = [("eval_samples", C.c_void_p), ("ray_trace", C.c_void_p)]
 
 
+class SvxBatchGrid(C.Structure):
+    _fields_ = [("grid", SvxGrid), ("grads", SvxGridGrads), ("accum", C.c_void_p), ("accum_stride", C.c_int32),
+                ("norm", C.c_float), ("beta", C.c_float), ("sparsity", C.c_float)]
+
+
 class SvxTable(C.Structure):
     _fields_ = [("data", C.c_void_p), ("dtype", C.c_int32), ("n_rows", C.c_int64), ("n_cols", C.c_int32)]
 
@@ -99,6 +104,8 @@ SIGNATURES = {
                                       P(SvxGridGrads), P(SvxRenderStats), _vp],
     "svx_volume_render_cuvol_fused_noalloc": [P(SvxGrid), P(SvxRays), P(SvxRenderOpts), _vp, _f32, _f32, _vp,
                                               P(SvxGridGrads), P(SvxRenderStats), _vp],
+    "svx_render_batch": [_i32, _vp, _i32, _i32, _vp, _vp, _vp, _vp, _i64, P(SvxRenderOpts), _vp, _vp, _vp, _vp],
+    "svx_camera_rays": [P(SvxCamera), _vp, _vp, _vp],
     "svx_sample_grid": [P(SvxGrid), _vp, _i64, _i32, _vp, _vp, _vp],
     "svx_sample_grid_backward": [P(SvxGrid), _vp, _i64, _vp, _vp, _vp, _vp, _i32, _vp],
     "svx_tv_grad": [_vp, P(_i32), P(SvxTable), _i32, _i32, _f32, _i32, _f32, _i32, _f32, _f32, _vp, _vp],

@@ -100,6 +100,9 @@ struct IoP {
   float* accum;    // optional padded gradient rows [n_voxels][accum_stride] (SH coefficients, density, 0s)
   int accum_stride;
   const int* order;            // optional processing order of the rays (a permutation)
+  const svx_batch_grid_t* batch_grids;  // batch mode: per-grid descriptors (device)
+  const int32_t* ray_grid;              // batch mode: grid of each ray (device)
+  const long long* n_rays_dev;          // batch mode: ray count, read on the device
   unsigned long long* work;    // ray counter (zeroed by the host)
   unsigned long long* eval_count;
   unsigned long long* trace;
@@ -710,26 +713,63 @@ __device__ __forceinline__ void flush_list(int F, const float* fl_val, const int
   __syncwarp();
 }
 
+// Where a ray's gradients go: the call's buffers, or in a batch, its grid's.
+struct GridOut {
+  float* grad_density;
+  float* grad_sh;
+  uint8_t* mask;
+  float* accum;
+  int accum_stride;
+  float norm, beta, sparsity;
+};
+
+__device__ __forceinline__ void load_batch_grid(const svx_batch_grid_t* bg, int gi, GridP& g, GridOut& go) {
+  const svx_batch_grid_t& d = bg[gi];
+  g.density = d.grid.density_data;
+  g.sh = d.grid.sh_data;
+  g.links = d.grid.links;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    g.size[i] = d.grid.size[i];
+    g.offset[i] = d.grid.offset[i];
+    g.scaling[i] = d.grid.scaling[i];
+  }
+  g.offy = d.grid.size[2];
+  g.offx = (long long)d.grid.size[1] * d.grid.size[2];
+  go.grad_density = d.grads.grad_density_out;
+  go.grad_sh = d.grads.grad_sh_out;
+  go.mask = d.grads.mask_out;
+  go.accum = d.accum;
+  go.accum_stride = d.accum_stride;
+  go.norm = d.norm;
+  go.beta = d.beta;
+  go.sparsity = d.sparsity;
+}
+
 // ---------------------------------------------------------------- kernel
 
-template <int BD, typename ShT, int MODE, bool IMAGE>
-__global__ void __launch_bounds__(kThreads) render_kernel(GridP g, OptP opt, IoP io) {
+template <int BD, typename ShT, int MODE, bool IMAGE, bool MULTI>
+__global__ void __launch_bounds__(kThreads) render_kernel(GridP g0, OptP opt, IoP io) {
   constexpr int C = 3 * BD;
   extern __shared__ float4 smem4[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   float* wbase = reinterpret_cast<float*>(smem4) + (size_t)wib * warp_smem_floats(C, io.cap);
   const WarpSmem sm = carve(wbase, C, io.cap);
-  const ShT* __restrict__ sh = reinterpret_cast<const ShT*>(g.sh);
   const int grp = lane >> 3, cj = lane & 7;
+  const long long n_rays = MULTI ? *io.n_rays_dev : io.n_rays;
 
   unsigned long long evals = 0;
   unsigned long long next = 0;
   if (lane == 0) next = atomicAdd(io.work, 1ull);
   next = __shfl_sync(kFull, next, 0);
 
-  while (next < (unsigned long long)io.n_rays) {
+  while (next < (unsigned long long)n_rays) {
     const long long ray = io.order != nullptr ? (long long)__ldg(io.order + next) : (long long)next;
+    GridP g = g0;
+    GridOut go{io.grad_density, io.grad_sh, io.mask, io.accum, io.accum_stride, io.norm, io.beta, io.sparsity};
+    if (MULTI) load_batch_grid(io.batch_grids, __ldg(io.ray_grid + ray), g, go);
+    const ShT* __restrict__ sh = reinterpret_cast<const ShT*>(g.sh);
     if (lane == 0) next = atomicAdd(io.work, 1ull);  // prefetch the following ray
     // ---- ray setup (all lanes, redundantly)
     float org[3], dir[3];
@@ -866,9 +906,9 @@ __global__ void __launch_bounds__(kThreads) render_kernel(GridP g, OptP opt, IoP
       float gout0, gout1, gout2;
       if (MODE == kFused) {
         // residual of the MSE loss (cuvol.cu:735-741)
-        gout0 = __fmul_rn(__fsub_rn(out0, __ldg(io.rgb_gt + ray * 3 + 0)), io.norm);
-        gout1 = __fmul_rn(__fsub_rn(out1, __ldg(io.rgb_gt + ray * 3 + 1)), io.norm);
-        gout2 = __fmul_rn(__fsub_rn(out2, __ldg(io.rgb_gt + ray * 3 + 2)), io.norm);
+        gout0 = __fmul_rn(__fsub_rn(out0, __ldg(io.rgb_gt + ray * 3 + 0)), go.norm);
+        gout1 = __fmul_rn(__fsub_rn(out1, __ldg(io.rgb_gt + ray * 3 + 1)), go.norm);
+        gout2 = __fmul_rn(__fsub_rn(out2, __ldg(io.rgb_gt + ray * 3 + 2)), go.norm);
       } else {
         gout0 = __ldg(io.grad_out + ray * 3 + 0);
         gout1 = __ldg(io.grad_out + ray * 3 + 1);
@@ -876,10 +916,10 @@ __global__ void __launch_bounds__(kThreads) render_kernel(GridP g, OptP opt, IoP
       }
       // light that passes the last sample: background, plus the beta-loss term (cuvol.cu:259-264)
       float carry = __fmul_rn(tb, __fadd_rn(__fadd_rn(gout0, gout1), gout2));
-      if (MODE == kFused && io.beta > 0.f) {
+      if (MODE == kFused && go.beta > 0.f) {
         const float tin = expf(lt_fwd);
         const double f = 1.0 - (double)tin / __dadd_rn((double)__fsub_rn(1.f, tin), 1e-3);
-        carry = __fadd_rn(carry, (float)((double)io.beta * f));
+        carry = __fadd_rn(carry, (float)((double)go.beta * f));
       }
 
       // ---- reverse pass over checkpointed segments
@@ -961,9 +1001,9 @@ __global__ void __launch_bounds__(kThreads) render_kernel(GridP g, OptP opt, IoP
           if (lane == 31) excl = 0.f;
           const float after = __fadd_rn(carry, excl);
           float gsig = __fmul_rn(s.ws, __fsub_rn(__fmul_rn(tc, tn), after));
-          if (io.sparsity > 0.f) {
+          if (go.sparsity > 0.f) {
             const float sg = s.sigma;
-            gsig = fmaf(io.sparsity, __fdiv_rn(__fmul_rn(4.f, sg), __fadd_rn(1.f, __fmul_rn(2.f, __fmul_rn(sg, sg)))),
+            gsig = fmaf(go.sparsity, __fdiv_rn(__fmul_rn(4.f, sg), __fadd_rn(1.f, __fmul_rn(2.f, __fmul_rn(sg, sg)))),
                         gsig);
           }
           carry = __fadd_rn(carry, __shfl_sync(kFull, incl, 0));
@@ -998,10 +1038,10 @@ __global__ void __launch_bounds__(kThreads) render_kernel(GridP g, OptP opt, IoP
                 // old corners not shared with the new cell: those on the faces -d moved across
                 const unsigned retire = near ? new_corner_mask(-dx, -dy, -dz) : 0xFFu;
                 if (F + 8 > kFlushCap) {
-                  if (io.accum != nullptr)
-                    flush_list_vec<BD>(F, fl_val, fl_link, sm.basis, io.accum, io.accum_stride, io.mask, lane);
+                  if (go.accum != nullptr)
+                    flush_list_vec<BD>(F, fl_val, fl_link, sm.basis, go.accum, go.accum_stride, go.mask, lane);
                   else
-                    flush_list<BD>(F, fl_val, fl_link, my_basis, io.grad_sh, io.grad_density, io.mask, lane);
+                    flush_list<BD>(F, fl_val, fl_link, my_basis, go.grad_sh, go.grad_density, go.mask, lane);
                   F = 0;
                 }
                 list_retiring(retire, B, lk_lane, fl_val, fl_link, F, lane);
@@ -1019,20 +1059,20 @@ __global__ void __launch_bounds__(kThreads) render_kernel(GridP g, OptP opt, IoP
             }
             B = __fadd_rn(B, sm.slot[q * kSlotStride + lane]);
           }
-          if (io.accum != nullptr)
-            flush_list_vec<BD>(F, fl_val, fl_link, sm.basis, io.accum, io.accum_stride, io.mask, lane);
+          if (go.accum != nullptr)
+            flush_list_vec<BD>(F, fl_val, fl_link, sm.basis, go.accum, go.accum_stride, go.mask, lane);
           else
-            flush_list<BD>(F, fl_val, fl_link, my_basis, io.grad_sh, io.grad_density, io.mask, lane);
+            flush_list<BD>(F, fl_val, fl_link, my_basis, go.grad_sh, go.grad_density, go.mask, lane);
         }
       }
       if (have_b) {
         float* fl_val = sm.tile;
         int* fl_link = reinterpret_cast<int*>(sm.tile + kFlushCap * 4);
         list_retiring(0xFFu, B, lk_lane, fl_val, fl_link, 0, lane);
-        if (io.accum != nullptr)
-          flush_list_vec<BD>(8, fl_val, fl_link, sm.basis, io.accum, io.accum_stride, io.mask, lane);
+        if (go.accum != nullptr)
+          flush_list_vec<BD>(8, fl_val, fl_link, sm.basis, go.accum, go.accum_stride, go.mask, lane);
         else
-          flush_list<BD>(8, fl_val, fl_link, my_basis, io.grad_sh, io.grad_density, io.mask, lane);
+          flush_list<BD>(8, fl_val, fl_link, my_basis, go.grad_sh, go.grad_density, go.mask, lane);
       }
     }
     __syncwarp();
@@ -1113,10 +1153,10 @@ __global__ void __launch_bounds__(256) add_accum_kernel(const float* __restrict_
 
 int g_cap = kDefaultCap;
 
-template <int BD, typename ShT, int MODE, bool IMAGE>
+template <int BD, typename ShT, int MODE, bool IMAGE, bool MULTI>
 int launch_t(const GridP& g, const OptP& opt, IoP io, long long n_rays, cudaStream_t st) {
   constexpr int C = 3 * BD;
-  auto kern = render_kernel<BD, ShT, MODE, IMAGE>;
+  auto kern = render_kernel<BD, ShT, MODE, IMAGE, MULTI>;
   const int cap = MODE == kFwd ? 0 : io.cap;
   io.cap = cap;
   const size_t smem = sizeof(float) * (size_t)warp_smem_floats(C, cap) * kWarps;
@@ -1146,19 +1186,22 @@ int launch_t(const GridP& g, const OptP& opt, IoP io, long long n_rays, cudaStre
   return SVX_OK;
 }
 
-template <int MODE, bool IMAGE>
-int dispatch(const svx_grid_t* grid, const GridP& g, const OptP& opt, const IoP& io, long long n,
-             cudaStream_t st) {
-  const int bd = grid->basis_dim;
-  const int dt = grid->sh_dtype;
+template <int MODE, bool IMAGE, bool MULTI = false>
+int dispatch_bd(int bd, int dt, const GridP& g, const OptP& opt, const IoP& io, long long n, cudaStream_t st) {
 #define SVX_CASE(BDV, T)                                   \
-  if (bd == BDV && dt == SvxDt<T>::v) return launch_t<BDV, T, MODE, IMAGE>(g, opt, io, n, st);
+  if (bd == BDV && dt == SvxDt<T>::v) return launch_t<BDV, T, MODE, IMAGE, MULTI>(g, opt, io, n, st);
   SVX_CASE(9, float) SVX_CASE(9, __nv_bfloat16) SVX_CASE(9, __half)
   SVX_CASE(4, float) SVX_CASE(4, __nv_bfloat16) SVX_CASE(4, __half)
   SVX_CASE(1, float) SVX_CASE(1, __nv_bfloat16) SVX_CASE(1, __half)
 #undef SVX_CASE
   set_error("unsupported basis_dim %d / sh dtype %d", bd, dt);
   return SVX_ERR_UNSUPPORTED;
+}
+
+template <int MODE, bool IMAGE>
+int dispatch(const svx_grid_t* grid, const GridP& g, const OptP& opt, const IoP& io, long long n,
+             cudaStream_t st) {
+  return dispatch_bd<MODE, IMAGE, false>(grid->basis_dim, grid->sh_dtype, g, opt, io, n, st);
 }
 
 }  // namespace
@@ -1517,4 +1560,87 @@ extern "C" int svx_volume_render_cuvol_fused_noalloc(const svx_grid_t* grid, con
   io.cap = g_cap;
   io.work = scratch;  // cleared on the stream by the launch, before the kernel
   return dispatch<kFused, false>(grid, g, o, io, rays->n_rays, as_stream(stream));
+}
+
+// ---------------------------------------------------------------- serving batches
+
+__global__ void __launch_bounds__(256) camera_rays_kernel(IoP io, long long n, float* __restrict__ origins,
+                                                          float* __restrict__ dirs) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    float org[3], dir[3];
+    camera_ray((int)(i % io.width), (int)(i / io.width), io, dir, org);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      origins[i * 3 + j] = org[j];
+      dirs[i * 3 + j] = dir[j];
+    }
+  }
+}
+
+extern "C" int svx_camera_rays(const svx_camera_t* cam, float* origins, float* dirs, void* stream) {
+  clear_error();
+  SVX_REQUIRE(cam != nullptr, SVX_ERR_INVALID, "camera is null");
+  SVX_REQUIRE(cam->width >= 0 && cam->height >= 0, SVX_ERR_INVALID, "negative image size");
+  SVX_REQUIRE(cam->c2w_rows == 3 || cam->c2w_rows == 4, SVX_ERR_INVALID, "c2w must have 3 or 4 rows");
+  const long long n = (long long)cam->width * cam->height;
+  if (n == 0) return SVX_OK;
+  SVX_REQUIRE(cam->c2w && origins && dirs, SVX_ERR_INVALID, "c2w / origins / dirs are null");
+  IoP io{};
+  io.c2w = cam->c2w;
+  io.fx = cam->fx;
+  io.fy = cam->fy;
+  io.cx = cam->cx;
+  io.cy = cam->cy;
+  io.ndcx = cam->ndc_coeffx;
+  io.ndcy = cam->ndc_coeffy;
+  io.width = cam->width;
+  long long blocks = (n + 255) / 256;
+  if (blocks > (long long)num_sms() * 16) blocks = (long long)num_sms() * 16;
+  camera_rays_kernel<<<(unsigned)blocks, 256, 0, as_stream(stream)>>>(io, n, origins, dirs);
+  SVX_LAUNCH_CHECK("camera_rays_kernel");
+  return SVX_OK;
+}
+
+extern "C" int svx_render_batch(int32_t mode, const svx_batch_grid_t* grids, int32_t basis_dim, int32_t sh_dtype,
+                                const float* origins, const float* dirs, const int32_t* ray_grid,
+                                const int64_t* n_rays_dev, int64_t max_rays, const svx_render_opts_t* opt,
+                                const float* rgb_gt, float* rgb_out, uint64_t* work, void* stream) {
+  clear_error();
+  SVX_REQUIRE(mode == 0 || mode == 1, SVX_ERR_INVALID, "mode %d: 0 (render) or 1 (fused)", mode);
+  SVX_REQUIRE(basis_dim == 9, SVX_ERR_UNSUPPORTED, "batched launches are built for basis_dim 9");
+  SVX_REQUIRE(max_rays >= 0, SVX_ERR_INVALID, "max_rays < 0");
+  if (max_rays == 0) return SVX_OK;
+  SVX_REQUIRE(grids && origins && dirs && ray_grid && n_rays_dev && rgb_out && work, SVX_ERR_INVALID,
+              "null batch buffer");
+  SVX_REQUIRE(mode == 0 || rgb_gt != nullptr, SVX_ERR_INVALID, "rgb_gt is null");
+  OptP o;
+  int rc = make_opt(opt, &o);
+  if (rc) return rc;
+  IoP io{};
+  io.origins = origins;
+  io.dirs = dirs;
+  io.n_rays = max_rays;
+  io.rgb_out = rgb_out;
+  io.rgb_gt = rgb_gt;
+  io.batch_grids = grids;
+  io.ray_grid = ray_grid;
+  io.n_rays_dev = reinterpret_cast<const long long*>(n_rays_dev);
+  io.work = reinterpret_cast<unsigned long long*>(work);
+  io.cap = g_cap;
+  GridP g{};  // per-ray grids come from the descriptors
+  cudaStream_t st = as_stream(stream);
+  switch (sh_dtype) {
+    case SVX_F32:
+      return mode == 0 ? launch_t<9, float, kFwd, false, true>(g, o, io, max_rays, st)
+                       : launch_t<9, float, kFused, false, true>(g, o, io, max_rays, st);
+    case SVX_BF16:
+      return mode == 0 ? launch_t<9, __nv_bfloat16, kFwd, false, true>(g, o, io, max_rays, st)
+                       : launch_t<9, __nv_bfloat16, kFused, false, true>(g, o, io, max_rays, st);
+    case SVX_F16:
+      return mode == 0 ? launch_t<9, __half, kFwd, false, true>(g, o, io, max_rays, st)
+                       : launch_t<9, __half, kFused, false, true>(g, o, io, max_rays, st);
+  }
+  set_error("sh_dtype %d unknown", sh_dtype);
+  return SVX_ERR_INVALID;
 }

@@ -80,18 +80,20 @@ def make_grid(reso, occupancy: Optional[float] = None, n_balls: int = 8, basis_d
         radii = torch.rand((n_balls,), generator=gen, dtype=torch.float64) * 0.2 + 0.1
         ratio = _ball_ratio(reso, centres, radii, device).flatten()
         k = max(int(round(occupancy * n3)), 1)
-        s = float(torch.kthvalue(ratio.cpu(), k).values)
+        s = float(torch.kthvalue(ratio, k).values)
         mask = (ratio <= s).view(reso).cpu()
+        del ratio
         links = torch.full(reso, -1, dtype=torch.int32)
         links[mask] = torch.arange(int(mask.sum()), dtype=torch.int32)
     N = n3 if mask is None else int(mask.sum())
     noise = torch.randn((N,), generator=gen, dtype=torch.float32)
     sh = torch.randn((N, 3 * basis_dim), generator=gen, dtype=torch.float32) * 0.3
     if density_mode == "ball":
-        X, Y, Z = voxel_centres(reso)
+        X, Y, Z = voxel_centres(reso, device=device)
         rad = torch.sqrt(X * X + Y * Y + Z * Z)
+        del X, Y, Z
         base = 40.0 * torch.clamp(1.0 - rad / 0.6, min=0.0)
-        base = base.flatten() if mask is None else base[mask]
+        base = (base.flatten() if mask is None else base[mask.to(base.device)]).cpu()
         density = torch.clamp(base + noise, min=0.0)
     elif density_mode == "normal53":
         density = torch.clamp(noise * 3.0 + 5.0, min=0.0)

@@ -351,7 +351,8 @@ def run_serve(args):
         server.add_grid(k, fresh(g), trainable=True)
     # warm-up: one request of each kind (graphs captured, kernels loaded), not timed
     warm = [server.submit(RenderRequest("g0", S.look_at_c2w((0.0, 0.0, -4.0)), 64, 64, fx=90.0)),
-            server.submit(TrainRequest("g0", *S.make_rays(4096, seed=1), tv_seed=0))]
+            server.submit(TrainRequest("g0", *S.make_rays(4096, seed=1), tv_seed=0)),
+            server.submit(TrainRequest("g1", *S.make_rays(65536, seed=2), tv_seed=0))]
     server.run_until_idle()
     for k, g in datas.items():          # back to the initial grids
         server.remove_grid(k)

@@ -202,12 +202,33 @@ typedef struct {
  *   n_rays_dev  device int64: rays processed by this launch (<= max_rays); it
  *               is read on the device, so that a captured CUDA graph of this
  *               call can be replayed for a new batch after the buffers change
+ *   order       NULL (rays in index order) or device int32 [max_rays]: the i-th
+ *               ray processed is order[i]; the first n_rays entries must be a
+ *               permutation of 0..n_rays-1 (see svx_ray_order).  Outputs stay
+ *               at each ray's own index.
  *   work        device uint64 scratch of the caller (cleared by the call)
  * Allocates nothing.  max_rays sizes the persistent grid. */
 int svx_render_batch(int32_t mode, const svx_batch_grid_t* grids, int32_t basis_dim, int32_t sh_dtype,
                      const float* origins, const float* dirs, const int32_t* ray_grid,
-                     const int64_t* n_rays_dev, int64_t max_rays, const svx_render_opts_t* opt,
-                     const float* rgb_gt, float* rgb_out, uint64_t* work, void* stream);
+                     const int32_t* order, const int64_t* n_rays_dev, int64_t max_rays,
+                     const svx_render_opts_t* opt, const float* rgb_gt, float* rgb_out, uint64_t* work,
+                     void* stream);
+
+/* Coherence order of a ray table against one grid: order_out[i] = index_base +
+ * the index of the i-th ray sorted by (octahedral direction bucket, Morton code
+ * of the chord midpoint inside the grid); rays that miss the grid go last.  This
+ * is the order the fused render uses internally for large batches; a caller that
+ * packs several requests into one svx_render_batch uses it per request.  Uses
+ * stream-ordered scratch (about 16 bytes per ray plus the sort's own). */
+int svx_ray_order(const svx_grid_t* grid, const svx_rays_t* rays, const svx_render_opts_t* opt,
+                  int32_t index_base, int32_t* order_out, void* stream);
+
+/* grad_sh[v, c] += accum[v, c] and grad_density[v] += accum[v, sh_data_dim] for
+ * every row v < n_voxels of a padded accumulation table [n_voxels, stride]
+ * (the accum of svx_batch_grid_t); rows that are all zero are skipped, so the
+ * untouched gradients keep their exact values.  Either output may be NULL. */
+int svx_add_accum(const float* accum, int32_t stride, int32_t sh_data_dim, int64_t n_voxels, float* grad_sh,
+                  float* grad_density, void* stream);
 
 /* The rays of a pinhole camera (what volume_render_cuvol_image marches,
  * cam2world_ray in svox2/csrc/include/render_util.cuh:526-544), written as

@@ -1098,7 +1098,8 @@ __device__ __forceinline__ unsigned spread_bits3(unsigned v) {
 
 __global__ void __launch_bounds__(256) ray_keys_kernel(GridP g, OptP opt, const float* __restrict__ origins,
                                                        const float* __restrict__ dirs, long long n,
-                                                       unsigned* __restrict__ keys, int* __restrict__ vals) {
+                                                       unsigned* __restrict__ keys, int* __restrict__ vals,
+                                                       int base) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
     float org[3], dir[3];
@@ -1129,7 +1130,7 @@ __global__ void __launch_bounds__(256) ray_keys_kernel(GridP g, OptP opt, const 
       key = ((qu << 2 | qv) << 24) | m;
     }
     keys[i] = key;
-    vals[i] = (int)i;
+    vals[i] = base + (int)i;
   }
 }
 
@@ -1300,6 +1301,46 @@ struct Scratch {
   }
 };
 
+// Sorts rays [0, n) by coherence key (ray_keys_kernel) and returns the permutation, offset by
+// base, in *order: written to out when it is non-null, else to scratch slot `slot` of scr.
+static int coherence_sort(const GridP& g, const OptP& o, const float* origins, const float* dirs, long long n,
+                          int base, int* out, Scratch& scr, int slot, int** order) {
+  SVX_REQUIRE(n < (1ll << 31) && (long long)base + n <= (1ll << 31), SVX_ERR_TOO_LARGE,
+              "%lld rays starting at index %d exceed the int32 order", n, base);
+  cudaStream_t st = scr.st;
+  size_t tmp_bytes = 0;
+  SVX_CUDA_TRY(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, (const unsigned*)nullptr, (unsigned*)nullptr,
+                                               (const int*)nullptr, (int*)nullptr, (int)n, 0, 32, st));
+  const size_t part = ((size_t)n * 4 + 255) & ~(size_t)255;
+  const size_t off_keys2 = part, off_vals = 2 * part, off_vals2 = 3 * part, off_tmp = 4 * part;
+  int rc = scr.alloc(slot, off_tmp + tmp_bytes);
+  if (rc) return rc;
+  char* buf = reinterpret_cast<char*>(scr.p[slot]);
+  unsigned* k_in = reinterpret_cast<unsigned*>(buf);
+  unsigned* k_out = reinterpret_cast<unsigned*>(buf + off_keys2);
+  int* v_in = reinterpret_cast<int*>(buf + off_vals);
+  int* v_out = out != nullptr ? out : reinterpret_cast<int*>(buf + off_vals2);
+  long long blocks = (n + 255) / 256;
+  if (blocks > (long long)num_sms() * 16) blocks = (long long)num_sms() * 16;
+  ray_keys_kernel<<<(unsigned)blocks, 256, 0, st>>>(g, o, origins, dirs, n, k_in, v_in, base);
+  SVX_LAUNCH_CHECK("ray_keys_kernel");
+  SVX_CUDA_TRY(cub::DeviceRadixSort::SortPairs(buf + off_tmp, tmp_bytes, k_in, k_out, v_in, v_out, (int)n, 0, 32,
+                                               st));
+  *order = v_out;
+  return SVX_OK;
+}
+
+static int launch_add_accum(const float* accum, int stride, int C, long long n_voxels, float* grad_sh,
+                            float* grad_density, cudaStream_t st) {
+  if (n_voxels <= 0 || (grad_sh == nullptr && grad_density == nullptr)) return SVX_OK;
+  long long blocks = (n_voxels + 7) / 8;
+  const long long cap = (long long)num_sms() * 32;
+  if (blocks > cap) blocks = cap;
+  add_accum_kernel<<<(unsigned)blocks, 256, 0, st>>>(accum, stride, C, n_voxels, grad_sh, grad_density);
+  SVX_LAUNCH_CHECK("add_accum_kernel");
+  return SVX_OK;
+}
+
 template <int MODE>
 static int render_rays(const svx_grid_t* grid, const svx_rays_t* rays, const svx_render_opts_t* opt,
                        IoP io, const svx_render_stats_t* stats, void* stream) {
@@ -1348,37 +1389,14 @@ static int render_rays(const svx_grid_t* grid, const svx_rays_t* rays, const svx
   }
   if (rays->n_rays >= kSortMinRays && rays->n_rays < (1ll << 31)) {
     // process the rays in coherence-key order
-    const long long n = rays->n_rays;
-    size_t tmp_bytes = 0;
-    SVX_CUDA_TRY(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, (const unsigned*)nullptr, (unsigned*)nullptr,
-                                                 (const int*)nullptr, (int*)nullptr, (int)n, 0, 32, st));
-    const size_t off_keys2 = ((size_t)n * 4 + 255) & ~(size_t)255;
-    const size_t off_vals = 2 * off_keys2, off_vals2 = 3 * off_keys2, off_tmp = 4 * off_keys2;
-    rc = scr.alloc(2, off_tmp + tmp_bytes);
+    int* order = nullptr;
+    rc = coherence_sort(g, o, rays->origins, rays->dirs, rays->n_rays, 0, nullptr, scr, 2, &order);
     if (rc) return rc;
-    char* base = reinterpret_cast<char*>(scr.p[2]);
-    unsigned* k_in = reinterpret_cast<unsigned*>(base);
-    unsigned* k_out = reinterpret_cast<unsigned*>(base + off_keys2);
-    int* v_in = reinterpret_cast<int*>(base + off_vals);
-    int* v_out = reinterpret_cast<int*>(base + off_vals2);
-    long long blocks = (n + 255) / 256;
-    if (blocks > (long long)num_sms() * 16) blocks = (long long)num_sms() * 16;
-    ray_keys_kernel<<<(unsigned)blocks, 256, 0, st>>>(g, o, rays->origins, rays->dirs, n, k_in, v_in);
-    SVX_LAUNCH_CHECK("ray_keys_kernel");
-    SVX_CUDA_TRY(cub::DeviceRadixSort::SortPairs(base + off_tmp, tmp_bytes, k_in, k_out, v_in, v_out, (int)n, 0, 32,
-                                                 st));
-    io.order = v_out;
+    io.order = order;
   }
   rc = dispatch<MODE, false>(grid, g, o, io, rays->n_rays, st);
   if (rc) return rc;
-  if (grads && grid->n_voxels > 0) {
-    long long blocks = (grid->n_voxels + 7) / 8;
-    const long long cap = (long long)num_sms() * 32;
-    if (blocks > cap) blocks = cap;
-    add_accum_kernel<<<(unsigned)blocks, 256, 0, st>>>(io.accum, stride, C, grid->n_voxels, io.grad_sh,
-                                                       io.grad_density);
-    SVX_LAUNCH_CHECK("add_accum_kernel");
-  }
+  if (grads) return launch_add_accum(io.accum, stride, C, grid->n_voxels, io.grad_sh, io.grad_density, st);
   return SVX_OK;
 }
 
@@ -1604,8 +1622,9 @@ extern "C" int svx_camera_rays(const svx_camera_t* cam, float* origins, float* d
 
 extern "C" int svx_render_batch(int32_t mode, const svx_batch_grid_t* grids, int32_t basis_dim, int32_t sh_dtype,
                                 const float* origins, const float* dirs, const int32_t* ray_grid,
-                                const int64_t* n_rays_dev, int64_t max_rays, const svx_render_opts_t* opt,
-                                const float* rgb_gt, float* rgb_out, uint64_t* work, void* stream) {
+                                const int32_t* order, const int64_t* n_rays_dev, int64_t max_rays,
+                                const svx_render_opts_t* opt, const float* rgb_gt, float* rgb_out, uint64_t* work,
+                                void* stream) {
   clear_error();
   SVX_REQUIRE(mode == 0 || mode == 1, SVX_ERR_INVALID, "mode %d: 0 (render) or 1 (fused)", mode);
   SVX_REQUIRE(basis_dim == 9, SVX_ERR_UNSUPPORTED, "batched launches are built for basis_dim 9");
@@ -1625,6 +1644,7 @@ extern "C" int svx_render_batch(int32_t mode, const svx_batch_grid_t* grids, int
   io.rgb_gt = rgb_gt;
   io.batch_grids = grids;
   io.ray_grid = ray_grid;
+  io.order = order;
   io.n_rays_dev = reinterpret_cast<const long long*>(n_rays_dev);
   io.work = reinterpret_cast<unsigned long long*>(work);
   io.cap = g_cap;
@@ -1643,4 +1663,33 @@ extern "C" int svx_render_batch(int32_t mode, const svx_batch_grid_t* grids, int
   }
   set_error("sh_dtype %d unknown", sh_dtype);
   return SVX_ERR_INVALID;
+}
+
+extern "C" int svx_ray_order(const svx_grid_t* grid, const svx_rays_t* rays, const svx_render_opts_t* opt,
+                             int32_t index_base, int32_t* order_out, void* stream) {
+  clear_error();
+  int rc = check_grid(grid);
+  if (rc) return rc;
+  SVX_REQUIRE(rays != nullptr, SVX_ERR_INVALID, "rays are null");
+  SVX_REQUIRE(rays->n_rays >= 0, SVX_ERR_INVALID, "n_rays < 0");
+  SVX_REQUIRE(index_base >= 0, SVX_ERR_INVALID, "index_base < 0");
+  if (rays->n_rays == 0) return SVX_OK;
+  SVX_REQUIRE(rays->origins && rays->dirs && order_out, SVX_ERR_INVALID, "origins / dirs / order_out are null");
+  OptP o;
+  rc = make_opt(opt, &o);
+  if (rc) return rc;
+  const GridP g = make_grid(grid);
+  Scratch scr(as_stream(stream));
+  int* order = nullptr;
+  return coherence_sort(g, o, rays->origins, rays->dirs, rays->n_rays, index_base, order_out, scr, 0, &order);
+}
+
+extern "C" int svx_add_accum(const float* accum, int32_t stride, int32_t sh_data_dim, int64_t n_voxels,
+                             float* grad_sh, float* grad_density, void* stream) {
+  clear_error();
+  SVX_REQUIRE(n_voxels >= 0, SVX_ERR_INVALID, "n_voxels < 0");
+  SVX_REQUIRE(sh_data_dim >= 0 && sh_data_dim + 1 <= stride && stride <= 32 && stride % 4 == 0, SVX_ERR_INVALID,
+              "stride %d must be a multiple of 4 in [sh_data_dim + 1, 32] (sh_data_dim %d)", stride, sh_data_dim);
+  SVX_REQUIRE(n_voxels == 0 || accum != nullptr, SVX_ERR_INVALID, "accum is null");
+  return launch_add_accum(accum, stride, sh_data_dim, n_voxels, grad_sh, grad_density, as_stream(stream));
 }

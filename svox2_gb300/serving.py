@@ -256,40 +256,6 @@ class Scheduler:
 
 # ---------------------------------------------------------------- GPU executor
 
-def _spread3(v: torch.Tensor, bits: int) -> torch.Tensor:
-    out = torch.zeros_like(v)
-    for b in range(bits):
-        out |= ((v >> b) & 1) << (3 * b)
-    return out
-
-
-def coherence_order(origins: torch.Tensor, dirs: torch.Tensor, grid) -> torch.Tensor:
-    """Permutation of rays by (direction bucket, Morton code of the chord midpoint), the order
-    the library uses for large batches: rays that run side by side are processed together."""
-    # scalars only: a host tensor copied to the device would wait for the stream's backlog
-    gsz = [float(v) for v in grid.links.shape]
-    off = [float(v) for v in (grid._offset * grid._grid_size() - 0.5).tolist()]
-    scl = [float(v) for v in (grid._scaling * grid._grid_size()).tolist()]
-    o = torch.stack([origins[:, i] * scl[i] + off[i] for i in range(3)], -1)
-    d = torch.stack([dirs[:, i] * scl[i] for i in range(3)], -1)
-    d = d / d.norm(dim=-1, keepdim=True)
-    inv = 1.0 / torch.where(d.abs() < 1e-9, torch.full_like(d, 1e-9), d)
-    t1 = (-0.5 - o) * inv
-    t2 = torch.stack([(gsz[i] - 0.5 - o[:, i]) for i in range(3)], -1) * inv
-    tmin = torch.minimum(t1, t2).amax(-1)
-    tmax = torch.maximum(t1, t2).amin(-1)
-    mid = o + (0.5 * (tmin + tmax)).unsqueeze(-1) * d
-    q = torch.stack([(mid[:, i] / gsz[i]).clamp(0, 0.999) for i in range(3)], -1).mul(256).long()
-    m = (_spread3(q[:, 0], 8) << 2) | (_spread3(q[:, 1], 8) << 1) | _spread3(q[:, 2], 8)
-    a = d / d.abs().sum(-1, keepdim=True)
-    u = torch.where(a[:, 2] >= 0, a[:, 0], (1 - a[:, 1].abs()) * torch.sign(a[:, 0]))
-    v = torch.where(a[:, 2] >= 0, a[:, 1], (1 - a[:, 0].abs()) * torch.sign(a[:, 1]))
-    qu = ((u + 1) * 2).long().clamp(0, 3)
-    qv = ((v + 1) * 2).long().clamp(0, 3)
-    key = (((qu << 2) | qv) << 24) | m
-    key = torch.where(tmin <= tmax, key, torch.full_like(key, 1 << 40))
-    return torch.argsort(key)
-
 def grid_bytes(grid, trainable: bool) -> int:
     n = grid.links.numel() * 4 + grid.density_data.numel() * 4 + grid.sh_data.numel() * grid.sh_data.element_size()
     if trainable:
@@ -330,6 +296,7 @@ class RenderServer:
                 "origins": torch.zeros((B, 3), device=dev), "dirs": torch.zeros((B, 3), device=dev),
                 "ray_grid": torch.zeros((B,), dtype=torch.int32, device=dev),
                 "rgb_gt": torch.zeros((B, 3), device=dev), "rgb_out": torch.zeros((B, 3), device=dev),
+                "order": torch.zeros((B,), dtype=torch.int32, device=dev),
                 "n_rays": torch.zeros((1,), dtype=torch.int64, device=dev),
                 "work": torch.zeros((4,), dtype=torch.int64, device=dev),
                 "desc": torch.zeros((max_grids, self.desc_size), dtype=torch.uint8, device=dev),
@@ -340,7 +307,7 @@ class RenderServer:
         self.sched.budget -= lane_bytes
         self.slots_free = list(range(max_grids))
         self.batches = {"render": 0, "train": 0}
-        self.sort_min_rays = 1 << 15
+        self.accum_min_rays = 1 << 15  # train steps this large accumulate into padded rows (vector atomics)
         self.lane_depth = 2          # batches a lane may have queued on the device
         # pinned staging for host->device updates (a pageable source would make the copy wait
         # for everything queued on the stream); a slot is reused once its copy has completed
@@ -362,7 +329,8 @@ class RenderServer:
         self.sched.add_grid(grid_id, grid_bytes(grid, trainable))
         self.dtype = grid.sh_data.dtype
         slot = self.slots_free.pop(0)
-        g = {"grid": grid, "slot": slot, "trainable": trainable}
+        from . import csrc
+        g = {"grid": grid, "slot": slot, "trainable": trainable, "struct": csrc._grid_struct(grid._to_cpp())}
         if trainable:
             N, Cc = grid.sh_data.shape
             g["mask"] = torch.zeros((N,), dtype=torch.bool, device=self.device)
@@ -376,11 +344,10 @@ class RenderServer:
         self.slots_free.append(self.grids.pop(grid_id)["slot"])
 
     def _set_desc(self, grid_id: str, norm: float, use_accum: bool = False) -> None:
-        from . import csrc
         _lib = self._lib
         g = self.grids[grid_id]
         d = _lib.SvxBatchGrid()
-        d.grid = csrc._grid_struct(g["grid"]._to_cpp())
+        d.grid = g["struct"]
         if g["trainable"]:
             gd, gs = g["grid"]._get_data_grads()
             d.grads = _lib.SvxGridGrads(gd.data_ptr(), gs.data_ptr(), g["mask"].data_ptr())
@@ -444,16 +411,8 @@ class RenderServer:
                 _lib.call("svx_camera_rays", C.byref(cam), t.buf["origins"].data_ptr(), t.buf["dirs"].data_ptr(),
                           lane["stream"].cuda_stream)
             else:
-                o = r.origins.to(self.device, non_blocking=True)
-                d = r.dirs.to(self.device, non_blocking=True)
-                gt = r.rgb_gt.to(self.device, non_blocking=True)
-                if t.n_rays >= self.sort_min_rays:
-                    perm = coherence_order(o, d, self.grids[t.grid_id]["grid"])
-                    o, d, gt = o[perm], d[perm], gt[perm]
-                    t.buf["perm"] = perm
-                t.buf["origins"] = o.contiguous()
-                t.buf["dirs"] = d.contiguous()
-                t.buf["rgb_gt"] = gt.contiguous()
+                for k in ("origins", "dirs", "rgb_gt"):
+                    t.buf[k] = getattr(r, k).to(self.device, non_blocking=True).contiguous()
                 t.buf["out"] = torch.empty((t.n_rays, 3), device=self.device)
 
     def _launch(self, name: str, n: int) -> None:
@@ -466,9 +425,11 @@ class RenderServer:
         dt = {torch.float32: _lib.SVX_F32, torch.bfloat16: _lib.SVX_BF16, torch.float16: _lib.SVX_F16}[self.dtype]
         mode = 0 if name == "render" else 1
 
+        order = lane["order"].data_ptr() if name == "train" else None
+
         def call():
             _lib.call("svx_render_batch", mode, lane["desc"].data_ptr(), 9, dt, lane["origins"].data_ptr(),
-                      lane["dirs"].data_ptr(), lane["ray_grid"].data_ptr(), lane["n_rays"].data_ptr(),
+                      lane["dirs"].data_ptr(), lane["ray_grid"].data_ptr(), order, lane["n_rays"].data_ptr(),
                       self.sched.batch_rays, C.byref(self.opt), lane["rgb_gt"].data_ptr(),
                       lane["rgb_out"].data_ptr(), lane["work"].data_ptr(), torch.cuda.current_stream().cuda_stream)
 
@@ -551,6 +512,7 @@ class RenderServer:
         return t.rays_launched >= t.n_rays and bool(t.rays_done_event) and all(e.query() for e in t.rays_done_event)
 
     def _run_train(self, trains: List[Ticket]) -> None:
+        _lib = self._lib
         lane = self.lanes["train"]
         st = lane["stream"]
         with torch.cuda.stream(st):
@@ -562,8 +524,12 @@ class RenderServer:
                 lane["dirs"][sl].copy_(t.buf["dirs"])
                 lane["rgb_gt"][sl].copy_(t.buf["rgb_gt"])
                 lane["ray_grid"][sl].fill_(g["slot"])
+                # each train step's rays run in coherence order (outputs stay at their own index)
+                rays = _lib.SvxRays(lane["origins"][sl].data_ptr(), lane["dirs"][sl].data_ptr(), t.n_rays)
+                _lib.call("svx_ray_order", C.byref(g["struct"]), C.byref(rays), C.byref(self.opt),
+                          off, lane["order"][sl].data_ptr(), st.cuda_stream)
                 g["mask"].zero_()
-                use_accum = t.n_rays >= self.sort_min_rays
+                use_accum = t.n_rays >= self.accum_min_rays
                 if use_accum:
                     g["accum"].zero_()
                 self._set_desc(t.grid_id, 2.0 / (3 * t.n_rays), use_accum)
@@ -574,18 +540,14 @@ class RenderServer:
             for t in trains:
                 g = self.grids[t.grid_id]
                 grid, r = g["grid"], t.request
-                out = lane["rgb_out"][off:off + t.n_rays]
-                if "perm" in t.buf:
-                    t.buf["out"][t.buf["perm"]] = out
-                else:
-                    t.buf["out"].copy_(out)
+                t.buf["out"].copy_(lane["rgb_out"][off:off + t.n_rays])
                 off += t.n_rays
                 if t.buf["accum"]:
                     # padded accumulation rows -> the grid's gradients
-                    Cc = grid.sh_data.size(1)
                     gd, gs = grid._get_data_grads()
-                    gs.add_(g["accum"][:, :Cc])
-                    gd.add_(g["accum"][:, Cc:Cc + 1])
+                    acc = g["accum"]
+                    _lib.call("svx_add_accum", acc.data_ptr(), acc.size(1), grid.sh_data.size(1), acc.size(0),
+                              gs.data_ptr(), gd.data_ptr(), st.cuda_stream)
                 # the rest of the reference's training step on this grid (opt/opt.py:557-595)
                 grid.sparse_grad_indexer = g["mask"]
                 grid.sparse_sh_grad_indexer = g["mask"].clone()

@@ -47,6 +47,13 @@ N_BALLS = 8
 Q = 1_000_000
 BYTES_PER_SAMPLE = 3648
 BYTES_PER_RAY = 48
+# DRAM bytes (read + write) per evaluated sample of render_kernel<9, float, fused> on this
+# workload: one ncu capture (--set full) of a 131,072-ray launch read 14.375 GB and wrote
+# 5.060 GB over 20,528,172 evaluated samples; scaled to a launch by its evaluated samples.
+DRAM_BYTES_PER_SAMPLE = 946.8
+# launches of this library per training step: ray_keys_kernel, 6 CUB radix-sort kernels,
+# render_kernel, add_accum_kernel, 2 x tv_sparse_kernel, 2 x step_mask_kernel
+LAUNCHES_PER_STEP = 13
 METRIC = "fused fwd+bwd rays/s at 256^3 SH9 (train step: render+MSE adjoint, TV, RMSprop)"
 WORKLOAD = "train step 256^3 20% occupancy SH9 FP32, 1M rays/step, fused fwd+bwd + TV + RMSprop"
 
@@ -146,7 +153,8 @@ def reset_state(grid, snapshot):
 
 
 def train_step(grid, rays_o, rays_d, gt, stats=None, ev=None):
-    """One step of the training loop; ev = (start, stop) events bracketing the fused render."""
+    """One step of the training loop; ev = (start, stop) events that the library records
+    around the ray-march kernel of the fused render."""
     from svox2_gb300 import Rays
     from svox2_gb300 import csrc as C
 
@@ -163,11 +171,10 @@ def train_step(grid, rays_o, rays_d, gt, stats=None, ev=None):
         holder.mask_out = grid.sparse_grad_indexer
         r = C.RaysSpec()
         r.origins, r.dirs = rays_o, rays_d
-        if ev is not None:
-            ev[0].record()
-        C.volume_render_cuvol_fused(grid._to_cpp(), r, grid.opt._to_cpp(), gt, 0.0, 0.0, rgb, holder, stats=stats)
-        if ev is not None:
-            ev[1].record()
+        st = dict(stats or {})
+        if ev is not None:      # recorded by the library just around the ray-march kernel
+            st["march_start"], st["march_stop"] = ev
+        C.volume_render_cuvol_fused(grid._to_cpp(), r, grid.opt._to_cpp(), gt, 0.0, 0.0, rgb, holder, stats=st)
         grid.sparse_sh_grad_indexer = grid.sparse_grad_indexer.clone()
     grid.inplace_tv_grad(grid.density_data.grad, scaling=1e-5, sparse_frac=0.01, contiguous=True)
     grid.inplace_tv_color_grad(grid.sh_data.grad, scaling=1e-3, sparse_frac=0.01, contiguous=True)
@@ -553,13 +560,16 @@ def emit(args, rank, world, g, value, e2e_val, total_ms, kern_ms, n_eval, clk):
                 g.density.shape[0]), "rays_per_step": Q, "l2": "no flush: grid + grads + RMS state 1.2 GB > L2",
                 "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
-                         "kernel": "render_kernel<9,float,fused>", "kernel_ms": kern_ms / args.steps,
-                         "eval_samples_per_step": n_eval / args.steps},
+                         "frac": achieved / peak, "traffic": DRAM_BYTES_PER_SAMPLE * n_eval / args.steps,
+                         "traffic_note": "DRAM bytes per launch, ncu capture of a 131k-ray launch scaled by "
+                                         "evaluated samples", "peak_kind": peak_kind,
+                         "kernel": "render_kernel<9,float,fused> (ray march + MSE adjoint)",
+                         "kernel_ms": kern_ms / args.steps, "eval_samples_per_step": n_eval / args.steps,
+                         "algorithmic_bytes_per_launch": alg_bytes},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_val, "unit": "rays/s", "h2d_bytes_per_step": 3 * Q * 3 * 4,
                     "d2h_bytes_per_step": Q * 3 * 4},
-            "gpu_launches": 5 * args.steps,
+            "gpu_launches": LAUNCHES_PER_STEP * args.steps,
             "clocks": clk.summary(),
         }
         print(json.dumps(line), flush=True)

@@ -115,10 +115,17 @@ typedef struct {
  *                 (sigma > sigma_thresh, before early stop) over the launch.
  *   ray_trace     device uint64 [n_rays]: per-ray hash of the sequence of
  *                 (cell, links, evaluated) decisions; lets tests compare the
- *                 sample indexing bit for bit with a CPU restatement. */
+ *                 sample indexing bit for bit with a CPU restatement.
+ *   march_start, march_stop
+ *                 cudaEvent_t handles of the caller (or NULL), recorded on the
+ *                 call's stream just before and just after the ray-march kernel,
+ *                 so that its duration can be told apart from the ray sort and
+ *                 the gradient flush around it. */
 typedef struct {
   uint64_t* eval_samples;
   uint64_t* ray_trace;
+  void* march_start;
+  void* march_stop;
 } svx_render_stats_t;
 
 /* ---- rendering: svox2/csrc/render_lerp_kernel_cuvol.cu ---------------- */

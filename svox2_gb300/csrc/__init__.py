@@ -201,6 +201,13 @@ def _stats_struct(stats) -> Optional[C.POINTER(_lib.SvxRenderStats)]:
     s = _lib.SvxRenderStats()
     s.eval_samples = _ptr(stats.get("eval_samples"))
     s.ray_trace = _ptr(stats.get("ray_trace"))
+    # torch.cuda.Event objects (timing enabled) recorded around the ray-march kernel
+    for key in ("march_start", "march_stop"):
+        ev = stats.get(key)
+        if ev is not None:
+            if ev.cuda_event == 0:        # torch creates the event lazily on first record
+                ev.record()
+            setattr(s, key, ev.cuda_event)
     return C.byref(s)
 
 

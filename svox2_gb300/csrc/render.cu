@@ -1341,6 +1341,14 @@ static int launch_add_accum(const float* accum, int stride, int C, long long n_v
   return SVX_OK;
 }
 
+// Records the caller's march_start / march_stop event (if any) on the stream.
+static int mark(const svx_render_stats_t* stats, bool stop, cudaStream_t st) {
+  if (stats == nullptr) return SVX_OK;
+  void* ev = stop ? stats->march_stop : stats->march_start;
+  if (ev != nullptr) SVX_CUDA_TRY(cudaEventRecord(reinterpret_cast<cudaEvent_t>(ev), st));
+  return SVX_OK;
+}
+
 template <int MODE>
 static int render_rays(const svx_grid_t* grid, const svx_rays_t* rays, const svx_render_opts_t* opt,
                        IoP io, const svx_render_stats_t* stats, void* stream) {
@@ -1394,7 +1402,11 @@ static int render_rays(const svx_grid_t* grid, const svx_rays_t* rays, const svx
     if (rc) return rc;
     io.order = order;
   }
+  rc = mark(stats, false, st);
+  if (rc) return rc;
   rc = dispatch<MODE, false>(grid, g, o, io, rays->n_rays, st);
+  if (rc) return rc;
+  rc = mark(stats, true, st);
   if (rc) return rc;
   if (grads) return launch_add_accum(io.accum, stride, C, grid->n_voxels, io.grad_sh, io.grad_density, st);
   return SVX_OK;
@@ -1484,7 +1496,11 @@ extern "C" int svx_volume_render_cuvol_image(const svx_grid_t* grid, const svx_c
   rc = scr.alloc(0, 256);
   if (rc) return rc;
   io.work = reinterpret_cast<unsigned long long*>(scr.p[0]);
-  return dispatch<kFwd, true>(grid, g, o, io, n, st);
+  rc = mark(stats, false, st);
+  if (rc) return rc;
+  rc = dispatch<kFwd, true>(grid, g, o, io, n, st);
+  if (rc) return rc;
+  return mark(stats, true, st);
 }
 
 extern "C" int svx_color_cache_capacity(void) { return svx::g_cap; }
@@ -1577,7 +1593,12 @@ extern "C" int svx_volume_render_cuvol_fused_noalloc(const svx_grid_t* grid, con
   io.trace = stats ? reinterpret_cast<unsigned long long*>(stats->ray_trace) : nullptr;
   io.cap = g_cap;
   io.work = scratch;  // cleared on the stream by the launch, before the kernel
-  return dispatch<kFused, false>(grid, g, o, io, rays->n_rays, as_stream(stream));
+  cudaStream_t st = as_stream(stream);
+  rc = mark(stats, false, st);
+  if (rc) return rc;
+  rc = dispatch<kFused, false>(grid, g, o, io, rays->n_rays, st);
+  if (rc) return rc;
+  return mark(stats, true, st);
 }
 
 // ---------------------------------------------------------------- serving batches

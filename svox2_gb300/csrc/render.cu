@@ -261,7 +261,7 @@ __device__ __forceinline__ float skip_dist(int32_t link, const int l[3], const f
 // slots 1..32 hold this segment's runs.
 constexpr int kSlots = 33;
 constexpr int kSlotStride = 33;  // floats per slot (odd: lanes reading different slots hit different banks)
-constexpr int kTileRows = 32;    // coefficient rows gathered per pass (one row per lane in the reduction)
+constexpr int kTileRows = 16;    // coefficient rows gathered per pass (one row per lane in the reduction)
 constexpr int kMaxRows = 8 * 32; // corner rows a segment can need
 constexpr int kFlushCap = 64;    // retiring corner rows listed before a flush pass
 
@@ -749,7 +749,10 @@ __device__ __forceinline__ void load_batch_grid(const svx_batch_grid_t* bg, int 
 // ---------------------------------------------------------------- kernel
 
 template <int BD, typename ShT, int MODE, bool IMAGE, bool MULTI>
-__global__ void __launch_bounds__(kThreads) render_kernel(GridP g0, OptP opt, IoP io) {
+// 128 registers and 13.8 KB of shared memory per warp (SH9, colour cache of 192 samples)
+// let four blocks (16 warps) share an SM; the march is latency-bound, so resident warps
+// count for more than the registers a larger budget would save.
+__global__ void __launch_bounds__(kThreads, 4) render_kernel(GridP g0, OptP opt, IoP io) {
   constexpr int C = 3 * BD;
   extern __shared__ float4 smem4[];
   const int lane = threadIdx.x & 31;

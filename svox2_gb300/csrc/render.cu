@@ -656,11 +656,11 @@ __device__ __forceinline__ void list_retiring(unsigned retire, float B, int lk_l
   }
 }
 
-// Vector flush into the padded rows: lane q adds channels 4q..4q+3 of a padded row
-// (SH coefficients 0..C-1, the density at C, then zeros) with one float4 atomic add,
-// ceil((C+1)/4) operations per corner row instead of C+1 scalar ones (the L2's
-// atomic throughput is counted in operations).  basis: the ray's SH basis in
-// shared memory.
+// Vector flush into the padded rows: a padded row (SH coefficients 0..C-1, the density
+// at C, then zeros) takes nvec = stride / 4 float4 atomic adds, ceil((C+1)/4) operations
+// per corner row instead of C+1 scalar ones (the L2's atomic throughput is counted in
+// operations).  The warp flushes 32 / nvec rows per pass: lane = row * nvec + q adds
+// channels 4q..4q+3 of its row.  basis: the ray's SH basis in shared memory.
 template <int BD>
 __device__ __forceinline__ void flush_list_vec(int F, const float* fl_val, const int* fl_link, const float* basis,
                                                float* __restrict__ accum, int stride, uint8_t* __restrict__ mask,
@@ -668,26 +668,26 @@ __device__ __forceinline__ void flush_list_vec(int F, const float* fl_val, const
   constexpr int C = 3 * BD;
   __syncwarp();
   const int nvec = stride >> 2;
+  const int per = 32 / nvec;
+  const int sub = lane / nvec, q = lane - sub * nvec;
   float coef[4];
   int grp[4];
 #pragma unroll
   for (int e = 0; e < 4; ++e) {
-    const int c = 4 * lane + e;
+    const int c = 4 * q + e;
     coef[e] = c < C ? basis[c % BD] : 1.f;
     grp[e] = c < C ? c / BD : (c == C ? 3 : 4);
   }
-  for (int f = 0; f < F; ++f) {
+  for (int f = sub; f - sub < F; f += per) {
+    if (sub >= per || f >= F) continue;
     const int lk = fl_link[f];
     if (lk < 0) continue;
-    if (lane < nvec) {
-      float x[4];
+    float x[4];
 #pragma unroll
-      for (int e = 0; e < 4; ++e) x[e] = grp[e] < 4 ? __fmul_rn(coef[e], fl_val[f * 4 + grp[e]]) : 0.f;
-      if (x[0] != 0.f || x[1] != 0.f || x[2] != 0.f || x[3] != 0.f)
-        atomicAdd(reinterpret_cast<float4*>(accum + (long long)lk * stride) + lane, make_float4(x[0], x[1], x[2], x[3]));
-    } else if (lane == 31 && mask != nullptr) {
-      mask[lk] = 1;
-    }
+    for (int e = 0; e < 4; ++e) x[e] = grp[e] < 4 ? __fmul_rn(coef[e], fl_val[f * 4 + grp[e]]) : 0.f;
+    if (x[0] != 0.f || x[1] != 0.f || x[2] != 0.f || x[3] != 0.f)
+      atomicAdd(reinterpret_cast<float4*>(accum + (long long)lk * stride) + q, make_float4(x[0], x[1], x[2], x[3]));
+    if (q == 0 && mask != nullptr) mask[lk] = 1;
   }
   __syncwarp();
 }

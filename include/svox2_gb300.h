@@ -315,6 +315,17 @@ int svx_sgd_step(void* data, int32_t data_dtype, float* grad, int64_t n_rows,
                  int32_t n_cols, int32_t indexer_kind, const void* indexer,
                  int64_t n_index, float lr, float lr_last, void* stream);
 
+/* ---- empty-space skipping: svox2/csrc/misc_kernel.cu ------------------- */
+
+/* accel_dist_prop (svox2/csrc/svox2.cpp:54, misc_kernel.cu:108-181 and 356-416;
+ * SparseGrid.accelerate, svox2/svox2.py:1487-1494).  Rewrites, in place, every
+ * negative entry of the int32 links table [size0, size1, size2] as -(1 + e), e
+ * being the number of consecutive empty levels (no voxel with a link >= 0)
+ * above the voxel in a pyramid that halves each side, rounding up, while all
+ * sides are > 1.  Entries >= 0 are unchanged.  Uses stream-ordered scratch of
+ * about 1/7 byte per voxel. */
+int svx_accel_dist_prop(int32_t* links, const int32_t size[3], void* stream);
+
 /* ---- library ------------------------------------------------------------ */
 
 /* Message of the last failed call on this thread ("" if none). */

@@ -210,3 +210,13 @@ def optim(rmsprop: bool, data, rms, grad, kind: int, indexer=None, beta=0.9, lr=
        C.c_void_p(_p(index)), C.c_int64(0 if index is None else index.shape[0]), C.c_float(beta), C.c_float(lr),
        C.c_float(eps), C.c_float(minval), C.c_float(lr_last))
     return data, rms, grad
+
+
+def accel_dist_prop(links: np.ndarray) -> np.ndarray:
+    """accel_dist_prop on a copy of an int32 [X, Y, Z] links table; returns the new links."""
+    out = np.ascontiguousarray(links, dtype=np.int32).copy()
+    size = (C.c_int * 3)(*out.shape)
+    fn = lib().oracle_accel_dist_prop
+    fn.restype = None
+    fn(C.c_void_p(out.ctypes.data), size)
+    return out

@@ -27,7 +27,7 @@ __all__ = [
     "SparseGridSpec", "RaysSpec", "CameraSpec", "RenderOptions", "GridOutputGrads",
     "volume_render_cuvol", "volume_render_cuvol_image", "volume_render_cuvol_backward",
     "volume_render_cuvol_fused", "sample_grid", "sample_grid_backward", "tv_grad",
-    "tv_grad_sparse", "rmsprop_step", "sgd_step",
+    "tv_grad_sparse", "rmsprop_step", "sgd_step", "accel_dist_prop",
 ]
 
 _DTYPES = {torch.float32: _lib.SVX_F32, torch.bfloat16: _lib.SVX_BF16, torch.float16: _lib.SVX_F16}
@@ -333,6 +333,14 @@ def _links_args(links: torch.Tensor):
     _check(not t.is_floating_point() and t.dtype == torch.int32, "links must be int32")
     _check(t.ndim == 3, "links must be 3-D")
     return t, (C.c_int32 * 3)(*t.shape)
+
+
+def accel_dist_prop(grid: torch.Tensor) -> None:
+    """svox2/csrc/misc_kernel.cu:356-416: empty-space skip levels written into the links
+    table in place (negative entries become -(1 + empty pyramid levels above))."""
+    lt, size = _links_args(grid)
+    with torch.cuda.device(lt.device):
+        _lib.call("svx_accel_dist_prop", lt.data_ptr(), size, _stream(lt.device))
 
 
 def tv_grad(links: torch.Tensor, data: torch.Tensor, start_dim: int, end_dim: int, scale: float,

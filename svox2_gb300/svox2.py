@@ -605,10 +605,62 @@ class SparseGrid(nn.Module):
             return torch.randint(0, grid_size, (sparse_num,), dtype=torch.int32, device=self.links.device)
         return None
 
-    # ---- not built here
-    def accelerate(self):
-        raise NotImplementedError("accelerate (accel_dist_prop empty-space skipping) is not built yet")
+    # ---- checkpoints (svox2/svox2.py:1526-1628): the reference's npz format
+    def save(self, path: str, compress: bool = False):
+        """Write radius, center, links, density_data, sh_data (stored as float16, as the
+        reference stores it) and basis_type to an npz file."""
+        save_fn = np.savez_compressed if compress else np.savez
+        data = {
+            "radius": self.radius.numpy(),
+            "center": self.center.numpy(),
+            "links": self.links.cpu().numpy(),
+            "density_data": self.density_data.data.cpu().numpy(),
+            # through float32 (exact for bfloat16 / float16) to the file's float16
+            "sh_data": self.sh_data.data.float().cpu().numpy().astype(np.float16),
+            "basis_type": self.basis_type,
+        }
+        save_fn(path, **data)
 
+    @classmethod
+    def load(cls, path: str, device: Union[torch.device, str] = "cpu",
+             sh_dtype: torch.dtype = torch.float32) -> "SparseGrid":
+        """Read a checkpoint written by save (or by the reference).  SH comes back as float32
+        like the reference, or kept in sh_dtype (bfloat16 / float16 storage); a grid placed on
+        a CUDA device is accelerated, as the reference does."""
+        z = np.load(path)
+        if "data" in z.keys():           # older single-table layout: [density | sh]
+            all_data = z.f.data
+            sh_data = all_data[..., 1:]
+            density_data = all_data[..., :1]
+        else:
+            sh_data = z.f.sh_data
+            density_data = z.f.density_data
+        if "background_data" in z:
+            raise NotImplementedError("checkpoints with the MSI background model are not supported by this build")
+        basis_type = z["basis_type"].item() if "basis_type" in z else BASIS_TYPE_SH
+        if basis_type != BASIS_TYPE_SH or "basis_data" in z.keys():
+            raise NotImplementedError("only SH-basis checkpoints are supported by this build")
+        radius = z.f.radius.tolist() if "radius" in z.files else [1.0, 1.0, 1.0]
+        center = z.f.center.tolist() if "center" in z.files else [0.0, 0.0, 0.0]
+        sh = torch.from_numpy(np.ascontiguousarray(sh_data.astype(np.float32)))
+        dens = torch.from_numpy(np.ascontiguousarray(density_data.astype(np.float32)))
+        links = torch.from_numpy(np.ascontiguousarray(z.f.links).astype(np.int32))
+        grid = cls.from_tables(links.to(device=device), dens.to(device=device),
+                               sh.to(device=device, dtype=sh_dtype), radius=radius, center=center)
+        if grid.links.is_cuda:
+            grid.accelerate()
+        return grid
+
+    # ---- empty-space skipping
+    def accelerate(self):
+        """Empty-space skip levels in the links table (svox2/svox2.py:1487-1494): every
+        negative link becomes -(1 + the empty levels of the 2x pyramid above it), which the
+        ray march turns into jumps over empty blocks."""
+        if not self.links.is_cuda:
+            raise RuntimeError("accelerate needs the grid on a CUDA device (there is no CPU path)")
+        _C.accel_dist_prop(self.links)
+
+    # ---- not built here
     def _unbuilt(self, *a, **k):
         raise NotImplementedError("this SparseGrid method is outside the GB300 build")
 

@@ -8,6 +8,7 @@ records inputs and outputs of
   * SparseGrid.volume_render(use_kernel=False) + autograd of F.mse_loss
     (svox2/svox2.py:658-884, the reference's gradcheck path), and
   * SparseGrid.sample(use_kernel=False) + autograd (svox2/svox2.py:576-653),
+  * SparseGrid.save / SparseGrid.load of a checkpoint (svox2/svox2.py:1526-1628),
 into tests/golden/*.npz.  sigma_thresh = stop_thresh = 0 so that the CPU
 path's semantics coincide with the CUDA kernel's (the reference's own
 test/test_render_gradcheck.py uses the same setting).
@@ -96,6 +97,28 @@ def sample_case(svox2, name, reso, basis_dim, n_points, seed):
     print(name, "points", n_points)
 
 
+def checkpoint_case(svox2, name, reso, basis_dim, occupancy, radius, center, seed):
+    """SparseGrid.save (svox2/svox2.py:1526-1553) of a seeded grid, written by the reference
+    itself, plus what the reference's SparseGrid.load (1555-1628) reads back from it."""
+    gen = torch.Generator().manual_seed(seed)
+    grid = svox2.SparseGrid(reso=reso, basis_dim=basis_dim, radius=radius, center=center, device="cpu")
+    keep = torch.rand(grid.links.shape, generator=gen) < occupancy
+    links = torch.full(grid.links.shape, -1, dtype=torch.int32)
+    links[keep] = torch.arange(int(keep.sum()), dtype=torch.int32)
+    N = int(keep.sum())
+    grid.links = links
+    grid.density_data = torch.nn.Parameter(torch.randn((N, 1), generator=gen) * 3.0)
+    grid.sh_data = torch.nn.Parameter(torch.randn((N, 3 * basis_dim), generator=gen) * 0.3)
+    path = OUT / f"ckpt_{name}.npz"
+    grid.save(str(path), compress=True)
+    back = svox2.SparseGrid.load(str(path), device="cpu")
+    np.savez_compressed(
+        OUT / f"ckpt_{name}_loaded.npz", links=back.links.numpy(), density_data=back.density_data.data.numpy(),
+        sh_data=back.sh_data.data.numpy(), radius=back.radius.numpy(), center=back.center.numpy(),
+        basis_dim=back.basis_dim, src_density=grid.density_data.data.numpy(), src_sh=grid.sh_data.data.numpy())
+    print(name, "checkpoint voxels", N)
+
+
 def main(ref_root: str):
     sys.path.insert(0, ref_root)
     warnings.filterwarnings("ignore")
@@ -106,6 +129,7 @@ def main(ref_root: str):
     render_case(svox2, "morton16_sh4", 16, 4, None, True, 40, 0.25, 0.7, 13)
     render_case(svox2, "dense10x12x14_sh1", (10, 12, 14), 1, None, False, 40, 0.0, 0.5, 14)
     sample_case(svox2, "dense10_sh9", 10, 9, 300, 15)
+    checkpoint_case(svox2, "sparse10x12x14_sh9", (10, 12, 14), 9, 0.4, [1.2, 0.8, 1.0], [0.1, -0.2, 0.3], 16)
 
 
 if __name__ == "__main__":

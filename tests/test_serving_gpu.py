@@ -82,7 +82,7 @@ def test_serving_matches_serial_replay():
                 assert torch.equal(rgb, t.result)
             touched.add(r.grid_id)
     for k in trainable:
-        assert float((ref[k].density_data - live[k].density_data).abs().max()) <= 1e-3
+        assert float((ref[k].density_data.detach() - live[k].density_data.detach()).abs().max()) <= 1e-3
     print("latency", latency_stats(tickets), "batches", server.batches)
 
 

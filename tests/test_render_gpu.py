@@ -254,6 +254,26 @@ def test_accelerated_links_skip():
     _run_fused(spec, og, rays_pair(o, d), o, d, gt, opt, oopt)
 
 
+def test_adjoint_sample_limit_is_enforced():
+    """A ray may need up to diagonal / step_size samples; beyond the adjoint's 64 x 64
+    checkpointed segments the fused and backward renders refuse on the host, the forward runs."""
+    from svox2_gb300 import csrc as C
+    g = S.make_grid(32, seed=30)
+    spec, og = grid_pair(g)
+    o, d, gt = S.make_rays(64, seed=31)
+    opt, _ = opt_struct(step=0.01)           # 32 * sqrt(3) / 0.01 ~ 5545 samples > 4096
+    rays = rays_pair(o, d)
+    N = og.density.shape[0]
+    grads = C.GridOutputGrads()
+    grads.grad_density_out = torch.zeros((N, 1), device="cuda")
+    grads.grad_sh_out = torch.zeros((N, og.sh.shape[1]), device="cuda")
+    grads.mask_out = torch.zeros((N,), dtype=torch.bool, device="cuda")
+    rgb = torch.zeros((64, 3), device="cuda")
+    with pytest.raises(RuntimeError, match="samples per ray"):
+        C.volume_render_cuvol_fused(spec, rays, opt, gt.cuda(), 0.0, 0.0, rgb, grads)
+    assert C.volume_render_cuvol(spec, rays, opt).shape == (64, 3)
+
+
 def test_invalid_arguments_raise():
     from svox2_gb300 import csrc as C
     g = S.make_grid(8, seed=18)

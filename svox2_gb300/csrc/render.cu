@@ -347,9 +347,8 @@ __device__ __forceinline__ void march_segment(Seg& s, float t0, float lt0, const
     const bool ok = lane == 0 ? (tk == t0) : (__fadd_rn(prev, opt.step) == tk);
     if (!__all_sync(kFull, ok)) {
       tk = t0;
-#pragma unroll
-      for (int i = 0; i < 31; ++i)
-        if (i < lane) tk = __fadd_rn(tk, opt.step);
+#pragma unroll 1
+      for (int i = 0; i < lane; ++i) tk = __fadd_rn(tk, opt.step);  // rare: kept compact
     }
   }
   const bool valid = tk <= r.tmax;
@@ -661,8 +660,10 @@ __device__ __forceinline__ void list_retiring(unsigned retire, float B, int lk_l
 // per corner row instead of C+1 scalar ones (the L2's atomic throughput is counted in
 // operations).  The warp flushes 32 / nvec rows per pass: lane = row * nvec + q adds
 // channels 4q..4q+3 of its row.  basis: the ray's SH basis in shared memory.
+// The flushes are kept out of line: the fused kernel calls them from six places, and at
+// this size its instruction fetch is part of what it waits on (out of line: 7% faster).
 template <int BD>
-__device__ __forceinline__ void flush_list_vec(int F, const float* fl_val, const int* fl_link, const float* basis,
+__device__ __noinline__ void flush_list_vec(int F, const float* fl_val, const int* fl_link, const float* basis,
                                                float* __restrict__ accum, int stride, uint8_t* __restrict__ mask,
                                                int lane) {
   constexpr int C = 3 * BD;
@@ -693,7 +694,7 @@ __device__ __forceinline__ void flush_list_vec(int F, const float* fl_val, const
 }
 
 template <int BD>
-__device__ __forceinline__ void flush_list(int F, const float* fl_val, const int* fl_link, float my_basis,
+__device__ __noinline__ void flush_list(int F, const float* fl_val, const int* fl_link, float my_basis,
                                            float* __restrict__ grad_sh, float* __restrict__ grad_density,
                                            uint8_t* __restrict__ mask, int lane) {
   constexpr int C = 3 * BD;

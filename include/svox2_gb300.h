@@ -162,6 +162,20 @@ int svx_volume_render_cuvol_fused(const svx_grid_t* grid, const svx_rays_t* rays
                                   const svx_grid_grads_t* grads,
                                   const svx_render_stats_t* stats, void* stream);
 
+/* volume_render_expected_term (svox2/csrc/svox2.cpp:25, render_lerp_kernel_cuvol.cu:122-176,
+ * 862-880, 1154-1172): out float32 [n_rays], the expected termination distance of each
+ * ray in world units, sum over evaluated samples of weight * (t / step_size) * world_step
+ * (0 for a ray that misses the grid). */
+int svx_volume_render_expected_term(const svx_grid_t* grid, const svx_rays_t* rays,
+                                    const svx_render_opts_t* opt, float* out, void* stream);
+
+/* volume_render_sigma_thresh (svox2/csrc/svox2.cpp:26, render_lerp_kernel_cuvol.cu:178-225,
+ * 882-902, 1174-1195): out float32 [n_rays], the distance of the first sample whose
+ * density exceeds sigma_thresh (0 if none). */
+int svx_volume_render_sigma_thresh(const svx_grid_t* grid, const svx_rays_t* rays,
+                                   const svx_render_opts_t* opt, float sigma_thresh, float* out,
+                                   void* stream);
+
 /* svx_volume_render_cuvol_fused_noalloc — no counterpart in the reference.
  * The fused render above for callers that cannot allocate device memory
  * while they run (work inside another framework's callbacks, hosts that plan

@@ -220,3 +220,18 @@ def accel_dist_prop(links: np.ndarray) -> np.ndarray:
     fn.restype = None
     fn(C.c_void_p(out.ctypes.data), size)
     return out
+
+
+def render_depth(grid: Grid, opt: Opt, origins, dirs, sigma_thresh=None, prec="f32", nthreads=None):
+    """volume_render_expected_term (sigma_thresh None) or volume_render_sigma_thresh: [Q]."""
+    R = _real(prec)
+    o = np.ascontiguousarray(origins, dtype=np.float32)
+    d = np.ascontiguousarray(dirs, dtype=np.float32)
+    out = np.zeros((o.shape[0],), dtype=R)
+    fn = getattr(lib(), "oracle_render_depth_" + prec)
+    fn.restype = None
+    gs, os_ = grid.struct(), opt.struct()
+    fn(C.byref(gs), C.byref(os_), C.c_void_p(o.ctypes.data), C.c_void_p(d.ctypes.data), C.c_int64(o.shape[0]),
+       C.c_int(0 if sigma_thresh is None else 1), C.c_float(0.0 if sigma_thresh is None else sigma_thresh),
+       C.c_void_p(out.ctypes.data), C.c_int(nthreads or default_threads()))
+    return out

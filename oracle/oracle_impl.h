@@ -397,6 +397,62 @@ void FN(oracle_render)(const oracle_grid_t* g, const oracle_opt_t* opt, const fl
   if (n_eval_total) *n_eval_total += total;
 }
 
+/* trace_ray_expected_term (render_lerp_kernel_cuvol.cu:122-176) and trace_ray_sigma_thresh
+ * (178-225): the expected termination distance sum w * (t / step) * world_step, or
+ * (threshold) the distance (t / step) * world_step of the first sample with sigma >
+ * sigma_thresh.  Neither applies last_sample_opaque. */
+static REAL FN(depth_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const REAL org[3], const REAL dir[3],
+                          int threshold, float sigma_thresh) {
+  const REAL log_stop = FN(log_stop)(opt->stop_thresh), step = (REAL)opt->step;
+  REAL t, lt = 0, outv = 0;
+  FN(ray_t) r;
+  FN(find_bounds)(&r, org, dir, g, opt);
+  if (r.tmin > r.tmax) return 0;
+  t = r.tmin;
+  while (t <= r.tmax) {
+    FN(sample_t) s;
+    FN(locate)(g, &r, t, &s);
+    if (s.lp[0] < -1) {
+      REAL skip = FN(skip_dist)(s.lp[0], s.l, s.pos, r.d);
+      if (skip >= step) {
+        t = t + CEIL(skip / step) * step;
+        continue;
+      }
+    }
+    {
+      const REAL sigma = FN(trilerp)(g, &s, g->density, 1, 0);
+      if (threshold) {
+        if (sigma > (REAL)sigma_thresh) return (t / step) * r.world_step;
+      } else if (sigma > (REAL)opt->sigma_thresh) {
+        const REAL pcnt = r.world_step * sigma;
+        const REAL w = EXP(lt) * ((REAL)1 - EXP(-pcnt));
+        lt = lt - pcnt;
+        outv = outv + w * (t / step) * r.world_step;
+        if (lt < log_stop) break;
+      }
+    }
+    t = t + step;
+  }
+  return outv;
+}
+
+void FN(oracle_render_depth)(const oracle_grid_t* g, const oracle_opt_t* opt, const float* origins,
+                             const float* dirs, int64_t Q, int threshold, float sigma_thresh, REAL* out,
+                             int nthreads) {
+  int64_t q;
+  if (nthreads < 1) nthreads = 1;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads)
+  for (q = 0; q < Q; ++q) {
+    REAL org[3], dir[3];
+    int i;
+    for (i = 0; i < 3; ++i) {
+      org[i] = (REAL)origins[q * 3 + i];
+      dir[i] = (REAL)dirs[q * 3 + i];
+    }
+    out[q] = FN(depth_ray)(g, opt, org, dir, threshold, sigma_thresh);
+  }
+}
+
 /* volume_render_cuvol_image, render_lerp_kernel_cuvol.cu:960-1008 (+ kernel 650-690). */
 void FN(oracle_render_image)(const oracle_grid_t* g, const oracle_opt_t* opt, const oracle_cam_t* cam, REAL* out,
                              uint64_t* trace, int nthreads) {

@@ -27,7 +27,8 @@ __all__ = [
     "SparseGridSpec", "RaysSpec", "CameraSpec", "RenderOptions", "GridOutputGrads",
     "volume_render_cuvol", "volume_render_cuvol_image", "volume_render_cuvol_backward",
     "volume_render_cuvol_fused", "sample_grid", "sample_grid_backward", "tv_grad",
-    "tv_grad_sparse", "rmsprop_step", "sgd_step", "accel_dist_prop",
+    "tv_grad_sparse", "rmsprop_step", "sgd_step", "accel_dist_prop", "volume_render_expected_term",
+    "volume_render_sigma_thresh",
 ]
 
 _DTYPES = {torch.float32: _lib.SVX_F32, torch.bfloat16: _lib.SVX_BF16, torch.float16: _lib.SVX_F16}
@@ -222,6 +223,32 @@ def volume_render_cuvol(grid: SparseGridSpec, rays: RaysSpec, opt: RenderOptions
     with torch.cuda.device(dev):
         _lib.call("svx_volume_render_cuvol", C.byref(g), C.byref(r), C.byref(_opt_struct(opt)),
                   out.data_ptr(), _stats_struct(stats), _stream(dev))
+    return out
+
+
+def volume_render_expected_term(grid: SparseGridSpec, rays: RaysSpec, opt: RenderOptions) -> torch.Tensor:
+    """svox2/csrc/render_lerp_kernel_cuvol.cu:1154-1172: expected termination distance [Q]."""
+    g = _grid_struct(grid)
+    dev = grid.sh_data.device
+    r = _rays_struct(rays, dev)
+    out = torch.empty((rays.origins.size(0),), dtype=torch.float32, device=dev)
+    with torch.cuda.device(dev):
+        _lib.call("svx_volume_render_expected_term", C.byref(g), C.byref(r), C.byref(_opt_struct(opt)),
+                  out.data_ptr(), _stream(dev))
+    return out
+
+
+def volume_render_sigma_thresh(grid: SparseGridSpec, rays: RaysSpec, opt: RenderOptions,
+                               sigma_thresh: float) -> torch.Tensor:
+    """svox2/csrc/render_lerp_kernel_cuvol.cu:1174-1195: distance of the first sample with
+    sigma > sigma_thresh [Q] (0 if none)."""
+    g = _grid_struct(grid)
+    dev = grid.sh_data.device
+    r = _rays_struct(rays, dev)
+    out = torch.empty((rays.origins.size(0),), dtype=torch.float32, device=dev)
+    with torch.cuda.device(dev):
+        _lib.call("svx_volume_render_sigma_thresh", C.byref(g), C.byref(r), C.byref(_opt_struct(opt)),
+                  float(sigma_thresh), out.data_ptr(), _stream(dev))
     return out
 
 

@@ -330,6 +330,7 @@ struct Seg {
   float pos[3];
   int l[3];
   long long base;   // linear index of the cell
+  float t;          // the sample's t
   float sigma, pcnt, ws, lt_before, lt_after;
 };
 
@@ -401,6 +402,7 @@ __device__ __forceinline__ void march_segment(Seg& s, float t0, float lt0, const
     dst[0] = make_int4(lk[0], lk[1], lk[2], lk[3]);
     dst[1] = make_int4(lk[4], lk[5], lk[6], lk[7]);
   }
+  s.t = tk;
   s.sigma = sigma;
   // last_sample_opaque: the final sample gets an infinite world step (cuvol.cu:79-81).
   s.ws = (opt.last_opaque && __fadd_rn(tk, opt.step) > r.tmax) ? 1e9f : r.world_step;
@@ -1085,6 +1087,67 @@ __global__ void __launch_bounds__(kThreads, 4) render_kernel(GridP g0, OptP opt,
   if (io.eval_count != nullptr && lane == 0 && evals) atomicAdd(io.eval_count, evals);
 }
 
+// ---------------------------------------------------------------- depth renders
+
+// volume_render_expected_term / volume_render_sigma_thresh (trace_ray_expected_term and
+// trace_ray_sigma_thresh, render_lerp_kernel_cuvol.cu:122-225): the ray's expected
+// termination distance, sum over evaluated samples of w * (t / step) * world_step, or
+// (THRESH) the distance of its first sample with sigma > thr.  Distances are along the
+// ray in world units.  One warp per ray, with the forward march's sampling and stop
+// rules; last_sample_opaque does not apply here, as in the reference.
+template <bool THRESH>
+__global__ void __launch_bounds__(kThreads) depth_kernel(GridP g, OptP opt, IoP io, float thr, float* __restrict__ out) {
+  __shared__ int slinks[kWarps][32 * 8];
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  OptP o = opt;
+  o.last_opaque = 0;
+  if (THRESH) {  // evaluated = sigma > thr, and no transmittance stop
+    o.sigma_thresh = thr;
+    o.log_stop = -INFINITY;
+  }
+  unsigned long long next = 0;
+  if (lane == 0) next = atomicAdd(io.work, 1ull);
+  next = __shfl_sync(kFull, next, 0);
+  while (next < (unsigned long long)io.n_rays) {
+    const long long ray = (long long)next;
+    if (lane == 0) next = atomicAdd(io.work, 1ull);
+    float org[3], dir[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      org[i] = __ldg(io.origins + ray * 3 + i);
+      dir[i] = __ldg(io.dirs + ray * 3 + i);
+    }
+    RayGeo rg;
+    find_bounds(rg, org, dir, g, o);
+    float acc = 0.f;
+    if (rg.tmin <= rg.tmax) {
+      float t = rg.tmin, lt = 0.f;
+      while (t <= rg.tmax) {
+        Seg s;
+        march_segment(s, t, lt, rg, g, o, slinks[wib], nullptr, lane);
+        if (THRESH) {
+          if (s.evm) {
+            const float tf = __shfl_sync(kFull, s.t, __ffs(s.evm) - 1);
+            acc = lane == 0 ? __fmul_rn(__fdiv_rn(tf, o.step), rg.world_step) : 0.f;
+            break;
+          }
+        } else if ((s.evm >> lane) & 1u) {
+          const float w = sample_weight(s.lt_before, s.pcnt);
+          acc = fmaf(__fmul_rn(w, __fdiv_rn(s.t, o.step)), rg.world_step, acc);
+        }
+        lt = s.lt_end;
+        if (s.stopped || s.end) break;
+        t = s.t_next;
+      }
+    }
+#pragma unroll
+    for (int d = 16; d >= 1; d >>= 1) acc = __fadd_rn(acc, __shfl_xor_sync(kFull, acc, d));
+    if (lane == 0) out[ray] = acc;
+    next = __shfl_sync(kFull, next, 0);
+  }
+}
+
 // ---------------------------------------------------------------- ray order
 
 // Coherence key of a ray: 4 bits of direction (2 x 2 bits of its octahedral map)
@@ -1717,4 +1780,51 @@ extern "C" int svx_add_accum(const float* accum, int32_t stride, int32_t sh_data
               "stride %d must be a multiple of 4 in [sh_data_dim + 1, 32] (sh_data_dim %d)", stride, sh_data_dim);
   SVX_REQUIRE(n_voxels == 0 || accum != nullptr, SVX_ERR_INVALID, "accum is null");
   return launch_add_accum(accum, stride, sh_data_dim, n_voxels, grad_sh, grad_density, as_stream(stream));
+}
+
+// volume_render_expected_term / volume_render_sigma_thresh host side
+// (render_lerp_kernel_cuvol.cu:1154-1195).
+static int render_depth(const svx_grid_t* grid, const svx_rays_t* rays, const svx_render_opts_t* opt, bool thresh,
+                        float thr, float* out, void* stream) {
+  clear_error();
+  int rc = check_grid(grid);
+  if (rc) return rc;
+  SVX_REQUIRE(rays != nullptr, SVX_ERR_INVALID, "rays are null");
+  SVX_REQUIRE(rays->n_rays >= 0, SVX_ERR_INVALID, "n_rays < 0");
+  if (rays->n_rays == 0) return SVX_OK;
+  SVX_REQUIRE(rays->origins && rays->dirs && out, SVX_ERR_INVALID, "origins / dirs / out are null");
+  OptP o;
+  rc = make_opt(opt, &o);
+  if (rc) return rc;
+  const GridP g = make_grid(grid);
+  IoP io{};
+  io.origins = rays->origins;
+  io.dirs = rays->dirs;
+  io.n_rays = rays->n_rays;
+  cudaStream_t st = as_stream(stream);
+  Scratch scr(st);
+  rc = scr.alloc(0, 256);
+  if (rc) return rc;
+  io.work = reinterpret_cast<unsigned long long*>(scr.p[0]);
+  SVX_CUDA_TRY(cudaMemsetAsync(io.work, 0, sizeof(unsigned long long), st));
+  long long blocks = (long long)num_sms() * 8;
+  const long long need = (rays->n_rays + kWarps - 1) / kWarps;
+  if (blocks > need) blocks = need;
+  if (thresh)
+    depth_kernel<true><<<(unsigned)blocks, kThreads, 0, st>>>(g, o, io, thr, out);
+  else
+    depth_kernel<false><<<(unsigned)blocks, kThreads, 0, st>>>(g, o, io, thr, out);
+  SVX_LAUNCH_CHECK("depth_kernel");
+  return SVX_OK;
+}
+
+extern "C" int svx_volume_render_expected_term(const svx_grid_t* grid, const svx_rays_t* rays,
+                                               const svx_render_opts_t* opt, float* out, void* stream) {
+  return render_depth(grid, rays, opt, false, 0.f, out, stream);
+}
+
+extern "C" int svx_volume_render_sigma_thresh(const svx_grid_t* grid, const svx_rays_t* rays,
+                                              const svx_render_opts_t* opt, float sigma_thresh, float* out,
+                                              void* stream) {
+  return render_depth(grid, rays, opt, true, sigma_thresh, out, stream);
 }

@@ -605,6 +605,22 @@ class SparseGrid(nn.Module):
             return torch.randint(0, grid_size, (sparse_num,), dtype=torch.int32, device=self.links.device)
         return None
 
+    # ---- depth renders (svox2/svox2.py:1181-1221)
+    def volume_render_depth(self, rays: Rays, sigma_thresh: Optional[float] = None):
+        """Per-ray distance along the ray (world units): the expected termination, or with
+        sigma_thresh the first point whose density strictly exceeds it.  Returns (N,)."""
+        if sigma_thresh is None:
+            return _C.volume_render_expected_term(self._to_cpp(), rays._to_cpp(), self.opt._to_cpp())
+        return _C.volume_render_sigma_thresh(self._to_cpp(), rays._to_cpp(), self.opt._to_cpp(), sigma_thresh)
+
+    def volume_render_depth_image(self, camera: Camera, sigma_thresh: Optional[float] = None,
+                                  batch_size: int = 5000):
+        """Depth image (H, W) of a camera, rays in batches of batch_size."""
+        rays = camera.gen_rays()
+        depths = [self.volume_render_depth(rays[b:b + batch_size], sigma_thresh)
+                  for b in range(0, camera.height * camera.width, batch_size)]
+        return torch.cat(depths, dim=0).view(camera.height, camera.width)
+
     # ---- checkpoints (svox2/svox2.py:1526-1628): the reference's npz format
     def save(self, path: str, compress: bool = False):
         """Write radius, center, links, density_data, sh_data (stored as float16, as the
@@ -665,6 +681,5 @@ class SparseGrid(nn.Module):
         raise NotImplementedError("this SparseGrid method is outside the GB300 build")
 
     resample = sparsify_background = resize = to_svox1 = _unbuilt
-    volume_render_depth = volume_render_depth_image = _unbuilt
     inplace_tv_lumisphere_grad = inplace_tv_background_grad = inplace_tv_basis_grad = _unbuilt
     inplace_l2_color_grad = optim_background_step = optim_basis_step = _unbuilt

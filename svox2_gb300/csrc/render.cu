@@ -662,6 +662,12 @@ __device__ __forceinline__ void list_retiring(unsigned retire, float B, int lk_l
 // per corner row instead of C+1 scalar ones (the L2's atomic throughput is counted in
 // operations).  The warp flushes 32 / nvec rows per pass: lane = row * nvec + q adds
 // channels 4q..4q+3 of its row.  basis: the ray's SH basis in shared memory.
+// Four-float atomic add whose result is not read (a reduction, no return value to wait for).
+__device__ __forceinline__ void red_add_v4(float4* p, float a, float b, float c, float d) {
+  asm volatile("red.relaxed.gpu.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(a), "f"(b), "f"(c), "f"(d)
+               : "memory");
+}
+
 // The flushes are kept out of line: the fused kernel calls them from six places, and at
 // this size its instruction fetch is part of what it waits on (out of line: 7% faster).
 template <int BD>
@@ -689,7 +695,7 @@ __device__ __noinline__ void flush_list_vec(int F, const float* fl_val, const in
 #pragma unroll
     for (int e = 0; e < 4; ++e) x[e] = grp[e] < 4 ? __fmul_rn(coef[e], fl_val[f * 4 + grp[e]]) : 0.f;
     if (x[0] != 0.f || x[1] != 0.f || x[2] != 0.f || x[3] != 0.f)
-      atomicAdd(reinterpret_cast<float4*>(accum + (long long)lk * stride) + q, make_float4(x[0], x[1], x[2], x[3]));
+      red_add_v4(reinterpret_cast<float4*>(accum + (long long)lk * stride) + q, x[0], x[1], x[2], x[3]);
     if (q == 0 && mask != nullptr) mask[lk] = 1;
   }
   __syncwarp();

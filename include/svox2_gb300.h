@@ -340,6 +340,20 @@ int svx_sgd_step(void* data, int32_t data_dtype, float* grad, int64_t n_rows,
  * about 1/7 byte per voxel. */
 int svx_accel_dist_prop(int32_t* links, const int32_t size[3], void* stream);
 
+/* dilate (svox2/csrc/svox2.cpp:53, misc_kernel.cu:20-48 and 335-350): out[v] =
+ * OR of the bool/uint8 grid [size0, size1, size2] over the 3x3x3 block around v,
+ * clamped at the faces.  out must not alias grid. */
+int svx_dilate(const uint8_t* grid, uint8_t* out, const int32_t size[3], void* stream);
+
+/* grid_weight_render (svox2/csrc/svox2.cpp:55-57, misc_kernel.cu:183-334 and 418-448):
+ * marches every pixel ray of cam through the dense float32 density grid data
+ * [size0, size1, size2] (world -> grid: grid = world * scaling + offset, host
+ * floats) and raises grid_weight (float32, same shape, >= 0 on entry) at the 8
+ * corners of each sample with sigma > 1e-8 to that sample's rendering weight. */
+int svx_grid_weight_render(const float* data, const int32_t size[3], const svx_camera_t* cam, float step_size,
+                           float stop_thresh, int32_t last_sample_opaque, const float offset[3],
+                           const float scaling[3], float* grid_weight, void* stream);
+
 /* ---- library ------------------------------------------------------------ */
 
 /* Message of the last failed call on this thread ("" if none). */

@@ -235,3 +235,35 @@ def render_depth(grid: Grid, opt: Opt, origins, dirs, sigma_thresh=None, prec="f
        C.c_int(0 if sigma_thresh is None else 1), C.c_float(0.0 if sigma_thresh is None else sigma_thresh),
        C.c_void_p(out.ctypes.data), C.c_int(nthreads or default_threads()))
     return out
+
+
+def dilate(mask: np.ndarray) -> np.ndarray:
+    """dilate (svox2/csrc/misc_kernel.cu:20-48): OR over the 3x3x3 block around each voxel,
+    clamped at the faces (numpy; boolean work, exact)."""
+    m = np.ascontiguousarray(mask, dtype=bool)
+    p = np.pad(m, 1, mode="edge")
+    out = np.zeros_like(m)
+    X, Y, Z = m.shape
+    for a in range(3):
+        for b in range(3):
+            for c in range(3):
+                out |= p[a:a + X, b:b + Y, c:c + Z]
+    return out
+
+
+def grid_weight_render(data, cam: dict, step_size, stop_thresh, last_opaque, offset, scaling, wmax=None,
+                       prec="f32"):
+    """grid_weight_render on a dense float32 density grid [X,Y,Z]; cam = dict(c2w [3|4,4], fx, fy,
+    cx, cy, width, height).  Returns the raised wmax (a new array unless given)."""
+    R = _real(prec)
+    d = np.ascontiguousarray(data, dtype=np.float32)
+    w = np.zeros(d.shape, dtype=R) if wmax is None else wmax
+    c2w = np.ascontiguousarray(cam["c2w"], dtype=np.float32)
+    oc = OCam(C.c_void_p(c2w.ctypes.data), cam["fx"], cam["fy"], cam["cx"], cam["cy"], cam["width"], cam["height"],
+              -1.0, -1.0)
+    fn = getattr(lib(), "oracle_grid_weight_render_" + prec)
+    fn.restype = None
+    fn(C.c_void_p(d.ctypes.data), (C.c_int * 3)(*d.shape), C.byref(oc), C.c_float(step_size),
+       C.c_float(stop_thresh), C.c_int(int(last_opaque)), (C.c_float * 3)(*offset), (C.c_float * 3)(*scaling),
+       C.c_void_p(w.ctypes.data))
+    return w

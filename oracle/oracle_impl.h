@@ -453,6 +453,76 @@ void FN(oracle_render_depth)(const oracle_grid_t* g, const oracle_opt_t* opt, co
   }
 }
 
+/* grid_weight_render, svox2/csrc/misc_kernel.cu:183-334 (grid_trace_ray + kernel): every pixel
+ * ray of the camera through the dense density grid data [X,Y,Z]; each sample with sigma > 1e-8
+ * raises wmax at its cell's 8 corners to the sample's weight.  The bounds and samples follow
+ * find_bounds / locate (the grid's transform, near clip 0). */
+void FN(oracle_grid_weight_render)(const float* data, const int size[3], const oracle_cam_t* cam, float step_size,
+                                   float stop_thresh, int last_opaque, const float offset[3],
+                                   const float scaling[3], REAL* wmax) {
+  oracle_grid_t g;
+  oracle_opt_t opt;
+  const REAL log_stop = FN(log_stop)(stop_thresh), step = (REAL)step_size;
+  const int64_t offy = size[2], offx = (int64_t)size[1] * size[2];
+  const int64_t co[8] = {0, 1, offy, offy + 1, offx, offx + 1, offx + offy, offx + offy + 1};
+  int64_t q, n = (int64_t)cam->width * cam->height;
+  int i;
+  g.links = NULL;
+  g.density = data;
+  g.sh = NULL;
+  g.n_voxels = 0;
+  g.basis_dim = 1;
+  for (i = 0; i < 3; ++i) {
+    g.size[i] = size[i];
+    g.offset[i] = offset[i];
+    g.scaling[i] = scaling[i];
+  }
+  opt.bg = 0.f;
+  opt.step = step_size;
+  opt.sigma_thresh = 0.f;
+  opt.stop_thresh = stop_thresh;
+  opt.near_clip = 0.f;
+  opt.spheric = 0;
+  opt.last_opaque = last_opaque;
+  for (q = 0; q < n; ++q) {
+    REAL org[3], dir[3], t, ll = 0;
+    FN(ray_t) r;
+    FN(camera_ray)((int)(q % cam->width), (int)(q / cam->width), cam, dir, org);
+    FN(find_bounds)(&r, org, dir, &g, &opt);
+    if (r.tmin > r.tmax) continue;
+    t = r.tmin;
+    while (t <= r.tmax) {
+      REAL pos[3], v[8], sigma;
+      int l[3], j;
+      int64_t idx;
+      for (j = 0; j < 3; ++j) {
+        REAL p = FMA(t, r.d[j], r.o[j]);
+        p = FMIN(FMAX(p, (REAL)0), (REAL)size[j] - (REAL)1);
+        l[j] = (int)p;
+        if (l[j] > size[j] - 2) l[j] = size[j] - 2;
+        pos[j] = p - (REAL)l[j];
+      }
+      idx = (int64_t)l[0] * offx + (int64_t)l[1] * offy + l[2];
+      for (j = 0; j < 8; ++j) v[j] = (REAL)data[idx + co[j]];
+      sigma = FN(lerp)(FN(lerp)(FN(lerp)(v[0], v[1], pos[2]), FN(lerp)(v[2], v[3], pos[2]), pos[1]),
+                       FN(lerp)(FN(lerp)(v[4], v[5], pos[2]), FN(lerp)(v[6], v[7], pos[2]), pos[1]), pos[0]);
+      if (last_opaque && t + step > r.tmax) {
+        sigma = sigma + (REAL)1e9f;
+        ll = 0;
+      }
+      if (sigma > (REAL)1e-8f) {
+        const REAL la = -(r.world_step * sigma);
+        const REAL w = EXP(ll) * ((REAL)1 - EXP(la));
+        ll = ll + la;
+        for (j = 0; j < 8; ++j)
+          if (w > wmax[idx + co[j]]) wmax[idx + co[j]] = w;
+        if (ll < log_stop) break;
+      }
+      t = t + step;
+    }
+  }
+}
+
 /* volume_render_cuvol_image, render_lerp_kernel_cuvol.cu:960-1008 (+ kernel 650-690). */
 void FN(oracle_render_image)(const oracle_grid_t* g, const oracle_opt_t* opt, const oracle_cam_t* cam, REAL* out,
                              uint64_t* trace, int nthreads) {

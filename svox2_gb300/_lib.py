@@ -113,6 +113,8 @@ SIGNATURES = {
     "svx_sample_grid": [P(SvxGrid), _vp, _i64, _i32, _vp, _vp, _vp],
     "svx_sample_grid_backward": [P(SvxGrid), _vp, _i64, _vp, _vp, _vp, _vp, _i32, _vp],
     "svx_accel_dist_prop": [_vp, P(_i32), _vp],
+    "svx_dilate": [_vp, _vp, P(_i32), _vp],
+    "svx_grid_weight_render": [_vp, P(_i32), P(SvxCamera), _f32, _f32, _i32, P(_f32), P(_f32), _vp, _vp],
     "svx_volume_render_expected_term": [P(SvxGrid), P(SvxRays), P(SvxRenderOpts), _vp, _vp],
     "svx_volume_render_sigma_thresh": [P(SvxGrid), P(SvxRays), P(SvxRenderOpts), _f32, _vp, _vp],
     "svx_tv_grad": [_vp, P(_i32), P(SvxTable), _i32, _i32, _f32, _i32, _f32, _i32, _f32, _f32, _vp, _vp],

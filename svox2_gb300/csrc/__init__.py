@@ -28,7 +28,7 @@ __all__ = [
     "volume_render_cuvol", "volume_render_cuvol_image", "volume_render_cuvol_backward",
     "volume_render_cuvol_fused", "sample_grid", "sample_grid_backward", "tv_grad",
     "tv_grad_sparse", "rmsprop_step", "sgd_step", "accel_dist_prop", "volume_render_expected_term",
-    "volume_render_sigma_thresh",
+    "volume_render_sigma_thresh", "dilate", "grid_weight_render",
 ]
 
 _DTYPES = {torch.float32: _lib.SVX_F32, torch.bfloat16: _lib.SVX_BF16, torch.float16: _lib.SVX_F16}
@@ -252,17 +252,21 @@ def volume_render_sigma_thresh(grid: SparseGridSpec, rays: RaysSpec, opt: Render
     return out
 
 
+def _camera_struct(cam: CameraSpec) -> _lib.SvxCamera:
+    c2w = _cuda_input(cam.c2w, "c2w")
+    _check(c2w.is_floating_point() and c2w.ndim == 2 and c2w.size(1) == 4 and c2w.size(0) in (3, 4),
+           "c2w must be float [3|4, 4]")
+    _check(c2w.dtype == torch.float32, "c2w must be float32")
+    return _lib.SvxCamera(c2w.data_ptr(), c2w.size(0), float(cam.fx), float(cam.fy), float(cam.cx), float(cam.cy),
+                          int(cam.width), int(cam.height), float(cam.ndc_coeffx), float(cam.ndc_coeffy))
+
+
 def volume_render_cuvol_image(grid: SparseGridSpec, cam: CameraSpec, opt: RenderOptions, *,
                               stats=None) -> torch.Tensor:
     """render_lerp_kernel_cuvol.cu:960-1008: image [H, W, 3] of a pinhole camera."""
     g = _grid_struct(grid)
     dev = grid.sh_data.device
-    c2w = _cuda_input(cam.c2w, "c2w")
-    _check(c2w.is_floating_point() and c2w.ndim == 2 and c2w.size(1) == 4 and c2w.size(0) in (3, 4),
-           "c2w must be float [3|4, 4]")
-    _check(c2w.dtype == torch.float32, "c2w must be float32")
-    c = _lib.SvxCamera(c2w.data_ptr(), c2w.size(0), float(cam.fx), float(cam.fy), float(cam.cx), float(cam.cy),
-                       int(cam.width), int(cam.height), float(cam.ndc_coeffx), float(cam.ndc_coeffy))
+    c = _camera_struct(cam)
     out = torch.empty((int(cam.height), int(cam.width), 3), dtype=torch.float32, device=dev)
     with torch.cuda.device(dev):
         _lib.call("svx_volume_render_cuvol_image", C.byref(g), C.byref(c), C.byref(_opt_struct(opt)),
@@ -368,6 +372,35 @@ def accel_dist_prop(grid: torch.Tensor) -> None:
     lt, size = _links_args(grid)
     with torch.cuda.device(lt.device):
         _lib.call("svx_accel_dist_prop", lt.data_ptr(), size, _stream(lt.device))
+
+
+def dilate(grid: torch.Tensor) -> torch.Tensor:
+    """svox2/csrc/misc_kernel.cu:335-350: 3x3x3 dilation of a bool [X, Y, Z] CUDA mask."""
+    t = _cuda_input(grid, "grid")
+    _check(not t.is_floating_point() and t.dtype == torch.bool and t.ndim == 3, "grid must be a 3-D bool tensor")
+    out = torch.empty_like(t)
+    with torch.cuda.device(t.device):
+        _lib.call("svx_dilate", t.data_ptr(), out.data_ptr(), (C.c_int32 * 3)(*t.shape), _stream(t.device))
+    return out
+
+
+def grid_weight_render(data: torch.Tensor, cam: CameraSpec, step_size: float, stop_thresh: float,
+                       last_sample_opaque: bool, offset: torch.Tensor, scaling: torch.Tensor,
+                       grid_weight: torch.Tensor) -> None:
+    """svox2/csrc/misc_kernel.cu:418-448: raise grid_weight [X, Y, Z] to the largest rendering
+    weight each voxel gets from the camera's rays through the dense density grid data."""
+    d = _cuda_input(data, "data")
+    w = _cuda_input(grid_weight, "grid_weight")
+    _check(d.dtype == torch.float32 and d.ndim == 3, "data must be float32 [X, Y, Z]")
+    _check(w.dtype == torch.float32 and w.shape == d.shape, "grid_weight must be float32 like data")
+    off = [float(v) for v in torch.as_tensor(offset).reshape(-1).tolist()]
+    scl = [float(v) for v in torch.as_tensor(scaling).reshape(-1).tolist()]
+    _check(len(off) == 3 and len(scl) == 3, "offset and scaling must have 3 elements")
+    c = _camera_struct(cam)
+    with torch.cuda.device(d.device):
+        _lib.call("svx_grid_weight_render", d.data_ptr(), (C.c_int32 * 3)(*d.shape), C.byref(c), float(step_size),
+                  float(stop_thresh), int(bool(last_sample_opaque)), (C.c_float * 3)(*off), (C.c_float * 3)(*scl),
+                  w.data_ptr(), _stream(d.device))
 
 
 def tv_grad(links: torch.Tensor, data: torch.Tensor, start_dim: int, end_dim: int, scale: float,

@@ -1,3 +1,6 @@
+// Grid editing kernels of svox2/csrc/misc_kernel.cu: empty-space skip levels
+// (accel_dist_prop) and 3-D mask dilation (dilate).
+//
 // Empty-space skip levels of a links table: accel_dist_prop
 // (svox2/csrc/misc_kernel.cu:108-181 kernels, 356-416 host; SparseGrid.accelerate,
 // svox2/svox2.py:1487-1494).
@@ -90,6 +93,24 @@ __global__ void __launch_bounds__(256) skip_levels_kernel(int32_t* __restrict__ 
   }
 }
 
+// dilate, misc_kernel.cu:20-48: out[v] = OR of grid over the 3x3x3 block around v, the block
+// clamped at the grid's faces.
+__global__ void __launch_bounds__(256) dilate_kernel(const uint8_t* __restrict__ in, int X, int Y, int Z,
+                                                     uint8_t* __restrict__ out) {
+  const long long n = (long long)X * Y * Z;
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < n;
+       v += (long long)gridDim.x * blockDim.x) {
+    const int z = (int)(v % Z), y = (int)((v / Z) % Y), x = (int)(v / ((long long)Y * Z));
+    uint8_t acc = 0;
+    for (int a = max(x - 1, 0); a <= min(x + 1, X - 1); ++a)
+      for (int b = max(y - 1, 0); b <= min(y + 1, Y - 1); ++b) {
+        const uint8_t* row = in + ((long long)a * Y + b) * Z;
+        for (int c = max(z - 1, 0); c <= min(z + 1, Z - 1); ++c) acc |= row[c];
+      }
+    out[v] = acc ? 1 : 0;
+  }
+}
+
 unsigned grid_blocks(long long n) {
   long long b = (n + 255) / 256;
   const long long cap = (long long)num_sms() * 32;
@@ -140,5 +161,19 @@ extern "C" int svx_accel_dist_prop(int32_t* links, const int32_t size[3], void* 
     set_error("launch of skip_levels_kernel failed: %s", cudaGetErrorString(e));
     return SVX_ERR_CUDA;
   }
+  return SVX_OK;
+}
+
+extern "C" int svx_dilate(const uint8_t* grid, uint8_t* out, const int32_t size[3], void* stream) {
+  clear_error();
+  SVX_REQUIRE(size != nullptr, SVX_ERR_INVALID, "size is null");
+  const int X = size[0], Y = size[1], Z = size[2];
+  SVX_REQUIRE(X >= 0 && Y >= 0 && Z >= 0, SVX_ERR_INVALID, "negative grid size");
+  const long long n = (long long)X * Y * Z;
+  if (n == 0) return SVX_OK;
+  SVX_REQUIRE(grid != nullptr && out != nullptr, SVX_ERR_INVALID, "grid / out is null");
+  SVX_REQUIRE(grid != out, SVX_ERR_INVALID, "dilate cannot run in place");
+  dilate_kernel<<<grid_blocks(n), 256, 0, as_stream(stream)>>>(grid, X, Y, Z, out);
+  SVX_LAUNCH_CHECK("dilate_kernel");
   return SVX_OK;
 }

@@ -1154,6 +1154,60 @@ __global__ void __launch_bounds__(kThreads) depth_kernel(GridP g, OptP opt, IoP 
   }
 }
 
+// ---------------------------------------------------------------- grid weight render
+
+// grid_weight_render (misc_kernel.cu:183-334): every pixel ray of a camera is marched through
+// a dense density grid data [X,Y,Z] (the resampled densities); each sample with sigma > 1e-8
+// raises grid_weight at its cell's 8 corners to the sample's weight, so grid_weight ends as
+// the largest weight any ray gave a voxel.  Weights are >= 0, so the maximum is taken on the
+// float bit patterns as integers.  One thread per pixel: the grids are small and the pass
+// runs once per camera during resampling.
+__global__ void __launch_bounds__(256) grid_weight_kernel(GridP g, OptP opt, IoP io, long long n_pix,
+                                                          const float* __restrict__ data,
+                                                          float* __restrict__ wmax) {
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n_pix;
+       q += (long long)gridDim.x * blockDim.x) {
+    float org[3], dir[3];
+    camera_ray((int)(q % io.width), (int)(q / io.width), io, dir, org);
+    RayGeo r;
+    find_bounds(r, org, dir, g, opt);
+    if (!(r.tmin <= r.tmax)) continue;
+    const long long co[8] = {0, 1, g.offy, g.offy + 1, g.offx, g.offx + 1, g.offx + g.offy, g.offx + g.offy + 1};
+    float ll = 0.f, t = r.tmin;
+    while (t <= r.tmax) {
+      int l[3];
+      float pos[3];
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        float p = fmaf(t, r.d[j], r.o[j]);
+        p = fminf(fmaxf(p, 0.f), (float)g.size[j] - 1.f);
+        l[j] = min((int)p, g.size[j] - 2);
+        pos[j] = __fsub_rn(p, (float)l[j]);
+      }
+      const long long idx = (long long)l[0] * g.offx + (long long)l[1] * g.offy + l[2];
+      float v[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) v[j] = __ldg(data + idx + co[j]);
+      float sigma = lerpf(lerpf(lerpf(v[0], v[1], pos[2]), lerpf(v[2], v[3], pos[2]), pos[1]),
+                          lerpf(lerpf(v[4], v[5], pos[2]), lerpf(v[6], v[7], pos[2]), pos[1]), pos[0]);
+      if (opt.last_opaque && __fadd_rn(t, opt.step) > r.tmax) {
+        sigma = __fadd_rn(sigma, 1e9f);
+        ll = 0.f;
+      }
+      if (sigma > 1e-8f) {
+        const float la = -__fmul_rn(r.world_step, sigma);
+        const float w = __fmul_rn(expf(ll), -expm1f(la));
+        ll = __fadd_rn(ll, la);
+        const int wi = __float_as_int(w);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) atomicMax(reinterpret_cast<int*>(wmax + idx + co[j]), wi);
+        if (ll < opt.log_stop) break;
+      }
+      t = __fadd_rn(t, opt.step);
+    }
+  }
+}
+
 // ---------------------------------------------------------------- ray order
 
 // Coherence key of a ray: 4 bits of direction (2 x 2 bits of its octahedral map)
@@ -1833,4 +1887,49 @@ extern "C" int svx_volume_render_sigma_thresh(const svx_grid_t* grid, const svx_
                                               const svx_render_opts_t* opt, float sigma_thresh, float* out,
                                               void* stream) {
   return render_depth(grid, rays, opt, true, sigma_thresh, out, stream);
+}
+
+extern "C" int svx_grid_weight_render(const float* data, const int32_t size[3], const svx_camera_t* cam,
+                                      float step_size, float stop_thresh, int32_t last_sample_opaque,
+                                      const float offset[3], const float scaling[3], float* grid_weight,
+                                      void* stream) {
+  clear_error();
+  SVX_REQUIRE(size != nullptr && cam != nullptr && offset != nullptr && scaling != nullptr, SVX_ERR_INVALID,
+              "size / camera / offset / scaling is null");
+  for (int i = 0; i < 3; ++i)
+    SVX_REQUIRE(size[i] >= 2, SVX_ERR_INVALID, "grid size[%d] = %d, each side must be >= 2", i, size[i]);
+  SVX_REQUIRE(cam->width >= 0 && cam->height >= 0, SVX_ERR_INVALID, "negative image size");
+  SVX_REQUIRE(cam->c2w_rows == 3 || cam->c2w_rows == 4, SVX_ERR_INVALID, "c2w must have 3 or 4 rows");
+  const long long n = (long long)cam->width * cam->height;
+  if (n == 0) return SVX_OK;
+  SVX_REQUIRE(data && grid_weight && cam->c2w, SVX_ERR_INVALID, "data / grid_weight / c2w is null");
+  svx_render_opts_t ro{};
+  ro.step_size = step_size;
+  ro.stop_thresh = stop_thresh;
+  ro.last_sample_opaque = last_sample_opaque;
+  OptP o;
+  int rc = make_opt(&ro, &o);
+  if (rc) return rc;
+  GridP g{};
+  for (int i = 0; i < 3; ++i) {
+    g.size[i] = size[i];
+    g.offset[i] = offset[i];
+    g.scaling[i] = scaling[i];
+  }
+  g.offy = size[2];
+  g.offx = (long long)size[1] * size[2];
+  IoP io{};
+  io.c2w = cam->c2w;
+  io.fx = cam->fx;
+  io.fy = cam->fy;
+  io.cx = cam->cx;
+  io.cy = cam->cy;
+  io.ndcx = cam->ndc_coeffx;
+  io.ndcy = cam->ndc_coeffy;
+  io.width = cam->width;
+  long long blocks = (n + 255) / 256;
+  if (blocks > (long long)num_sms() * 16) blocks = (long long)num_sms() * 16;
+  grid_weight_kernel<<<(unsigned)blocks, 256, 0, as_stream(stream)>>>(g, o, io, n, data, grid_weight);
+  SVX_LAUNCH_CHECK("grid_weight_kernel");
+  return SVX_OK;
 }

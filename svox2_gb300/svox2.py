@@ -621,6 +621,93 @@ class SparseGrid(nn.Module):
                   for b in range(0, camera.height * camera.width, batch_size)]
         return torch.cat(depths, dim=0).view(camera.height, camera.width)
 
+    # ---- resampling (svox2/svox2.py:1223-1424)
+    def resample(self, reso: Union[int, List[int]], sigma_thresh: float = 5.0, weight_thresh: float = 0.01,
+                 dilate: int = 2, cameras: Optional[List["Camera"]] = None, use_z_order: bool = False,
+                 accelerate: bool = True, weight_render_stop_thresh: float = 0.2, max_elements: int = 0):
+        """Resample the grid to reso and sparsify it.  The old grid is sampled at the new voxel
+        centres (grid coordinates); a voxel is kept if its density reaches sigma_thresh or, with
+        cameras, if its largest rendering weight over the cameras' rays reaches weight_thresh.
+        max_elements > 0 raises the threshold so at most that many voxels are kept.  The mask is
+        dilated `dilate` times, colours are sampled for the kept voxels only, and links are
+        rebuilt in raster (or Morton) order.  Optimiser state and gradients are dropped."""
+        if not self.links.is_cuda:
+            _no_cpu_path("SparseGrid.resample")
+        with torch.no_grad():
+            device = self.links.device
+            reso = [int(reso)] * 3 if isinstance(reso, int) else [int(r) for r in reso]
+            assert len(reso) == 3, "reso must be an integer or indexable object of 3 ints"
+            if use_z_order and not (reso[0] == reso[1] == reso[2] and utils.is_pow2(reso[0])):
+                print("Morton code requires a cube grid of power-of-2 size, ignoring...")
+                use_z_order = False
+            # new voxel centres in the current grid's coordinates
+            cur = self.links.shape
+            axes = []
+            for i in range(3):
+                f = 0.5 * cur[i] / reso[i]
+                axes.append(torch.linspace(f - 0.5, cur[i] - f - 0.5, reso[i], dtype=torch.float32))
+            X, Y, Z = torch.meshgrid(*axes, indexing="ij")
+            points = torch.stack((X, Y, Z), dim=-1).view(-1, 3)
+            morton = None
+            if use_z_order:
+                morton = utils.gen_morton(reso[0], dtype=torch.long).view(-1)
+                points[morton] = points.clone()
+            points = points.to(device=device)
+
+            batch = 720720
+            dens = torch.cat([self.sample(points[i:i + batch], grid_coords=True, want_colors=False)[0]
+                              for i in range(0, points.size(0), batch)], dim=0).view(reso)
+            self.density_data.grad = None
+            self.sh_data.grad = None
+            self.sparse_grad_indexer = None
+            self.sparse_sh_grad_indexer = None
+            self.density_rms = None
+            self.sh_rms = None
+
+            if cameras is not None:
+                gsz = torch.tensor(reso, dtype=torch.float32)
+                offset = self._offset * gsz - 0.5
+                scaling = self._scaling * gsz
+                wmax = torch.zeros(reso, dtype=torch.float32, device=device)
+                for cam in cameras:
+                    _C.grid_weight_render(dens, cam._to_cpp(), 0.5, weight_render_stop_thresh, False,
+                                          offset, scaling, wmax)
+                score, thresh = wmax, weight_thresh
+            else:
+                score, thresh = dens, sigma_thresh
+            mask = score >= thresh
+            if 0 < max_elements < score.numel() and max_elements < int(torch.count_nonzero(mask)):
+                bounded = torch.topk(score.view(-1), k=max_elements, sorted=False).values.min().item()
+                thresh = max(thresh, bounded)
+                mask = score >= thresh
+            if cameras is None and self.opt.last_sample_opaque:
+                mask[:, :, -1] = True          # keep the last z layer
+            del score
+            for _ in range(int(dilate)):
+                mask = _C.dilate(mask)
+            mask = mask.view(-1)
+            new_dens = dens.view(-1)[mask]
+            kept = points[mask]
+            cols = [self.sample(kept[i:i + batch], grid_coords=True, want_colors=True)[1]
+                    for i in range(0, kept.size(0), batch)]
+            new_sh = torch.cat(cols, dim=0) if cols else torch.empty_like(self.sh_data[:0])
+
+            if morton is not None:
+                inv = torch.empty_like(morton)
+                inv[morton] = torch.arange(morton.size(0), dtype=morton.dtype)
+                order = inv.to(device)[mask]
+                links = torch.full((mask.size(0),), -1, dtype=torch.int32, device=device)
+                links[order] = torch.arange(order.size(0), dtype=torch.int32, device=device)
+            else:
+                links = torch.cumsum(mask.to(torch.int32), dim=-1).to(torch.int32) - 1
+                links[~mask] = -1
+            self.capacity = int(new_dens.size(0))
+            self.density_data = nn.Parameter(new_dens.view(-1, 1).contiguous())
+            self.sh_data = nn.Parameter(new_sh.to(self.sh_data.dtype).contiguous())
+            self.links = links.view(reso).contiguous()
+            if accelerate:
+                self.accelerate()
+
     # ---- checkpoints (svox2/svox2.py:1526-1628): the reference's npz format
     def save(self, path: str, compress: bool = False):
         """Write radius, center, links, density_data, sh_data (stored as float16, as the
@@ -680,6 +767,6 @@ class SparseGrid(nn.Module):
     def _unbuilt(self, *a, **k):
         raise NotImplementedError("this SparseGrid method is outside the GB300 build")
 
-    resample = sparsify_background = resize = to_svox1 = _unbuilt
+    sparsify_background = resize = to_svox1 = _unbuilt
     inplace_tv_lumisphere_grad = inplace_tv_background_grad = inplace_tv_basis_grad = _unbuilt
     inplace_l2_color_grad = optim_background_step = optim_basis_step = _unbuilt

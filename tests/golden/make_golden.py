@@ -9,6 +9,7 @@ records inputs and outputs of
     (svox2/svox2.py:658-884, the reference's gradcheck path), and
   * SparseGrid.sample(use_kernel=False) + autograd (svox2/svox2.py:576-653),
   * SparseGrid.save / SparseGrid.load of a checkpoint (svox2/svox2.py:1526-1628),
+  * SparseGrid.resample on the CPU path without dilation (svox2/svox2.py:1223-1424),
 into tests/golden/*.npz.  sigma_thresh = stop_thresh = 0 so that the CPU
 path's semantics coincide with the CUDA kernel's (the reference's own
 test/test_render_gradcheck.py uses the same setting).
@@ -119,6 +120,29 @@ def checkpoint_case(svox2, name, reso, basis_dim, occupancy, radius, center, see
     print(name, "checkpoint voxels", N)
 
 
+def resample_case(svox2, name, reso, new_reso, occupancy, sigma_thresh, seed):
+    """SparseGrid.resample (svox2/svox2.py:1223-1424) on the CPU path: no dilation (the
+    reference's dilate needs its CUDA extension), density threshold, raster links."""
+    gen = torch.Generator().manual_seed(seed)
+    grid = svox2.SparseGrid(reso=reso, basis_dim=9, device="cpu")
+    keep = torch.rand(grid.links.shape, generator=gen) < occupancy
+    links = torch.full(grid.links.shape, -1, dtype=torch.int32)
+    links[keep] = torch.arange(int(keep.sum()), dtype=torch.int32)
+    N = int(keep.sum())
+    grid.links = links
+    dens = torch.rand((N, 1), generator=gen) * 20.0
+    sh = torch.randn((N, 27), generator=gen) * 0.3
+    grid.density_data = torch.nn.Parameter(dens.clone())
+    grid.sh_data = torch.nn.Parameter(sh.clone())
+    grid.resample(new_reso, sigma_thresh=sigma_thresh, dilate=0, cameras=None, use_z_order=False,
+                  accelerate=False)
+    np.savez_compressed(
+        OUT / f"resample_{name}.npz", src_links=links.numpy(), src_density=dens.numpy(), src_sh=sh.numpy(),
+        new_reso=np.array(new_reso), sigma_thresh=sigma_thresh, links=grid.links.numpy(),
+        density=grid.density_data.data.numpy(), sh=grid.sh_data.data.numpy())
+    print(name, "resampled voxels", grid.density_data.shape[0])
+
+
 def main(ref_root: str):
     sys.path.insert(0, ref_root)
     warnings.filterwarnings("ignore")
@@ -130,6 +154,7 @@ def main(ref_root: str):
     render_case(svox2, "dense10x12x14_sh1", (10, 12, 14), 1, None, False, 40, 0.0, 0.5, 14)
     sample_case(svox2, "dense10_sh9", 10, 9, 300, 15)
     checkpoint_case(svox2, "sparse10x12x14_sh9", (10, 12, 14), 9, 0.4, [1.2, 0.8, 1.0], [0.1, -0.2, 0.3], 16)
+    resample_case(svox2, "sparse12_to_9x14x11", 12, [9, 14, 11], 0.5, 4.0, 17)
 
 
 if __name__ == "__main__":

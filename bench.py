@@ -124,6 +124,20 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def max_over_ranks(ms: float, dist, device) -> float:
+    """The slowest replica's time (the job's time); ms itself without torch.distributed."""
+    if dist is None:
+        return ms
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(world: int, rays_per_step: int, steps: int, ms: float) -> float:
+    """Rays/s of the whole job: every replica processes rays_per_step rays per step (weak scaling)."""
+    return world * rays_per_step * steps / (ms / 1e3)
+
+
 def build_workload(device, seed_rays: int, n_batches: int):
     from svox2_gb300 import synthetic as S
     from svox2_gb300 import SparseGrid
@@ -493,10 +507,7 @@ def main():
     total_ms = t_start.elapsed_time(t_stop)
     kern_ms = sum(a.elapsed_time(b) for a, b in evs)
     n_eval = int(stats["eval_samples"].item())
-    if dist is not None:
-        tt = torch.tensor([total_ms], device=device)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total_ms = float(tt.item())
+    total_ms = max_over_ranks(total_ms, dist, device)
 
     # ---- e2e: public API, rays from pinned host memory, colours back to the host
     if args.skip_e2e:
@@ -504,8 +515,8 @@ def main():
     else:
         reset_state(grid, snapshot)   # both arms train from the same initial grid
         e2e_ms = run_e2e(args, grid, host_batches, device, n_batches, dist)
-    value = world * Q * args.steps / (total_ms / 1e3)
-    e2e_val = world * Q * args.steps / (e2e_ms / 1e3)
+    value = whole_job_rate(world, Q, args.steps, total_ms)
+    e2e_val = whole_job_rate(world, Q, args.steps, e2e_ms)
     emit(args, rank, world, g, value, e2e_val, total_ms, kern_ms, n_eval, clk)
     if dist is not None:
         dist.destroy_process_group()
@@ -533,10 +544,7 @@ def run_e2e(args, grid, host_batches, device, n_batches, dist):
     e_stop.record()
     torch.cuda.synchronize()
     e2e_ms = e_start.elapsed_time(e_stop)
-    if dist is not None:
-        tt = torch.tensor([e2e_ms], device=device)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_ms = float(tt.item())
+    e2e_ms = max_over_ranks(e2e_ms, dist, device)
     return e2e_ms
 
 

@@ -289,12 +289,14 @@ struct WarpSmem {
   float* col;        // [cap][3]
 };
 
-__host__ __device__ constexpr int warp_smem_floats(int C, int cap) {
-  return (32 * 8 + kSlots * kSlotStride + tile_floats(C) + 2 * kMaxRows + kSlots * 6 + 3 * kNumCkpt +
-          3 * kMaxStride + 12 + 3 * cap + 3) & ~3;
+// adjoint: the reverse pass's checkpoint arrays are carved (the forward-only kernel has none,
+// which lets five of its blocks share an SM).
+__host__ __device__ constexpr int warp_smem_floats(int C, int cap, bool adjoint = true) {
+  return (32 * 8 + kSlots * kSlotStride + tile_floats(C) + 2 * kMaxRows + kSlots * 6 +
+          (adjoint ? 3 * kNumCkpt + 3 * kMaxStride : 0) + 12 + 3 * cap + 3) & ~3;
 }
 
-__device__ __forceinline__ WarpSmem carve(float* base, int C, int cap) {
+__device__ __forceinline__ WarpSmem carve(float* base, int C, int cap, bool adjoint = true) {
   WarpSmem s;
   s.links = reinterpret_cast<int*>(base);
   s.slot = base + 32 * 8;
@@ -311,7 +313,7 @@ __device__ __forceinline__ WarpSmem carve(float* base, int C, int cap) {
   s.tmp_t = reinterpret_cast<float*>(s.ck_idx + kNumCkpt);
   s.tmp_lt = s.tmp_t + kMaxStride;
   s.tmp_idx = reinterpret_cast<int*>(s.tmp_lt + kMaxStride);
-  s.basis = reinterpret_cast<float*>(s.tmp_idx + kMaxStride);
+  s.basis = adjoint ? reinterpret_cast<float*>(s.tmp_idx + kMaxStride) : s.ck_t;
   s.col = s.basis + 12;
   return s;
 }
@@ -760,14 +762,15 @@ __device__ __forceinline__ void load_batch_grid(const svx_batch_grid_t* bg, int 
 template <int BD, typename ShT, int MODE, bool IMAGE, bool MULTI>
 // 128 registers and 13.8 KB of shared memory per warp (SH9, colour cache of 192 samples)
 // let four blocks (16 warps) share an SM; the march is latency-bound, so resident warps
-// count for more than the registers a larger budget would save.
-__global__ void __launch_bounds__(kThreads, 4) render_kernel(GridP g0, OptP opt, IoP io) {
+// count for more than the registers a larger budget would save.  The forward-only kernel
+// (no colour cache, no checkpoints: 10 KB per warp) fits five blocks at 102 registers.
+__global__ void __launch_bounds__(kThreads, MODE == kFwd ? 5 : 4) render_kernel(GridP g0, OptP opt, IoP io) {
   constexpr int C = 3 * BD;
   extern __shared__ float4 smem4[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
-  float* wbase = reinterpret_cast<float*>(smem4) + (size_t)wib * warp_smem_floats(C, io.cap);
-  const WarpSmem sm = carve(wbase, C, io.cap);
+  float* wbase = reinterpret_cast<float*>(smem4) + (size_t)wib * warp_smem_floats(C, io.cap, MODE != kFwd);
+  const WarpSmem sm = carve(wbase, C, io.cap, MODE != kFwd);
   const int grp = lane >> 3, cj = lane & 7;
   const long long n_rays = MULTI ? *io.n_rays_dev : io.n_rays;
 
@@ -1287,7 +1290,7 @@ int launch_t(const GridP& g, const OptP& opt, IoP io, long long n_rays, cudaStre
   auto kern = render_kernel<BD, ShT, MODE, IMAGE, MULTI>;
   const int cap = MODE == kFwd ? 0 : io.cap;
   io.cap = cap;
-  const size_t smem = sizeof(float) * (size_t)warp_smem_floats(C, cap) * kWarps;
+  const size_t smem = sizeof(float) * (size_t)warp_smem_floats(C, cap, MODE != kFwd) * kWarps;
   static std::mutex mu;
   static int blocks_per_sm[2][1024];  // indexed by device, cap/4 (0 = unset)
   int dev = 0;

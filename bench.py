@@ -272,7 +272,8 @@ def run_mixed(args):
     """Mixed-precision configuration: 512^3 grid, 8% occupancy (32 balls), SH stored
     as bfloat16 or float16 (density float32, all arithmetic float32) against the
     float32 form: PSNR of an 800x800 render from a fixed camera, relative error of
-    the fused-step gradients over 4M rays, and fused-step throughput."""
+    the fused-step gradients over 4M rays, fused-step throughput and forward-only render
+    throughput over the same rays."""
     from svox2_gb300 import Camera, Rays, SparseGrid
     from svox2_gb300 import synthetic as S
 
@@ -304,7 +305,19 @@ def run_mixed(args):
         e1.record()
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / args.steps
+        # forward-only render of the same rays (what a render request runs)
+        with torch.no_grad():
+            grid.volume_render(rays)
+            torch.cuda.synchronize()
+            f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            f0.record()
+            for _ in range(args.steps):
+                grid.volume_render(rays)
+            f1.record()
+            torch.cuda.synchronize()
+        fwd_ms = f0.elapsed_time(f1) / args.steps
         entry = {"rays_per_s": q / (ms / 1e3), "ms_per_step": ms,
+                 "render_rays_per_s": q / (fwd_ms / 1e3), "render_ms": fwd_ms,
                  "sh_bytes": int(grid.sh_data.numel() * grid.sh_data.element_size())}
         if ref_img is None:
             ref_img, ref_gd, ref_gs = img, gd, gs

@@ -34,7 +34,7 @@ extern "C" {
 typedef enum {
   SVX_OK = 0,
   SVX_ERR_INVALID = 1,      /* bad argument: null pointer, size, dtype, range */
-  SVX_ERR_UNSUPPORTED = 2,  /* feature outside this build (MSI background, MLP basis…) */
+  SVX_ERR_UNSUPPORTED = 2,  /* feature this library does not implement (MSI background, MLP basis…) */
   SVX_ERR_CUDA = 3,         /* a CUDA runtime call or kernel launch failed */
   SVX_ERR_TOO_LARGE = 4     /* size beyond a documented limit */
 } svx_status;

@@ -9,7 +9,7 @@ on the current PyTorch stream of the data's device and never synchronises
 the host (the reference used the legacy default stream, and ``sample_grid``
 created and synchronised two private streams per call).
 
-Operators the build leaves out (nvol/svox1 backends, MSI background,
+Operators this library leaves out (nvol/svox1 backends, MSI background,
 lumisphere TV, dilate, grid_weight_render, the ``tv`` value) are not
 exported, so ``name in csrc.__dict__`` checks like the reference's
 ``volume_render_image`` dispatch behave as with a module that lacks them.
@@ -139,7 +139,7 @@ def _grid_struct(grid: SparseGridSpec) -> _lib.SvxGrid:
     _check(dens.device == sh.device == links.device, "grid tensors must be on one device")
     _check(sh.size(0) == dens.size(0), "density_data and sh_data row counts differ")
     if grid.background_links is not None and grid.background_links.numel() > 0:
-        raise RuntimeError("MSI background (background_links) is not supported by this build")
+        raise RuntimeError("MSI background (background_links) is not supported by svox2_gb300")
     _check(off.numel() == 3 and scl.numel() == 3, "_offset and _scaling must have 3 elements")
     offv = off.to(torch.float32).tolist()
     sclv = scl.to(torch.float32).tolist()

@@ -86,7 +86,7 @@ __device__ __forceinline__ float lerpf(float a, float b, float w) {
 
 // 1 / |v| for the direction rescale (_get_delta_scale,
 // svox2/csrc/include/render_util.cuh:463-474).  The reference calls rnorm3df;
-// this build forms the norm from exact double products and rounds once more to
+// this library forms the norm from exact double products and rounds once more to
 // float, which any IEEE host reproduces exactly.
 __device__ __forceinline__ float rnorm3_exact(float x, float y, float z) {
   double s = __dadd_rn(__dadd_rn(__dmul_rn((double)x, (double)x), __dmul_rn((double)y, (double)y)),

@@ -28,7 +28,7 @@ from .defs import BASIS_TYPE_3D_TEXTURE, BASIS_TYPE_MLP, BASIS_TYPE_SH
 
 
 def _no_cpu_path(what: str):
-    raise RuntimeError(f"{what}: this build has no CPU path; the grid and rays must be on a CUDA device")
+    raise RuntimeError(f"{what}: svox2_gb300 has no CPU path; the grid and rays must be on a CUDA device")
 
 
 @dataclass
@@ -238,7 +238,7 @@ class SparseGrid(nn.Module):
     :param basis_dim: 1, 4 or 9 (SH degree 0, 1, 2)
     :param use_z_order: Morton order of the initial links (cubic power-of-2 grids)
     :param use_sphere_bound: allocate only voxels within the unit ball
-    :param background_nlayers: must be 0 (no MSI background in this build)
+    :param background_nlayers: must be 0 (svox2_gb300 has no MSI background)
     :param device: torch device
     :param sh_dtype: storage type of sh_data: torch.float32 (default), bfloat16 or float16
     """
@@ -739,10 +739,10 @@ class SparseGrid(nn.Module):
             sh_data = z.f.sh_data
             density_data = z.f.density_data
         if "background_data" in z:
-            raise NotImplementedError("checkpoints with the MSI background model are not supported by this build")
+            raise NotImplementedError("checkpoints with the MSI background model are not supported by svox2_gb300")
         basis_type = z["basis_type"].item() if "basis_type" in z else BASIS_TYPE_SH
         if basis_type != BASIS_TYPE_SH or "basis_data" in z.keys():
-            raise NotImplementedError("only SH-basis checkpoints are supported by this build")
+            raise NotImplementedError("only SH-basis checkpoints are supported by svox2_gb300")
         radius = z.f.radius.tolist() if "radius" in z.files else [1.0, 1.0, 1.0]
         center = z.f.center.tolist() if "center" in z.files else [0.0, 0.0, 0.0]
         sh = torch.from_numpy(np.ascontiguousarray(sh_data.astype(np.float32)))
@@ -765,7 +765,7 @@ class SparseGrid(nn.Module):
 
     # ---- not built here
     def _unbuilt(self, *a, **k):
-        raise NotImplementedError("this SparseGrid method is outside the GB300 build")
+        raise NotImplementedError("this SparseGrid method is not implemented in svox2_gb300")
 
     sparsify_background = resize = to_svox1 = _unbuilt
     inplace_tv_lumisphere_grad = inplace_tv_background_grad = inplace_tv_basis_grad = _unbuilt

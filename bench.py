@@ -536,25 +536,51 @@ def main():
 
 
 def run_e2e(args, grid, host_batches, device, n_batches, dist):
+    """The training step through the public grid API with host buffers: every step copies its
+    rays and targets from pinned host memory and reads its colours back.  The copies run on a
+    copy stream, double-buffered, so the next step's upload and the previous step's download
+    overlap the current step's kernels, as a training loop feeding the GPU would do."""
     pinned = [tuple(t.pin_memory() for t in b) for b in host_batches]
-    dbuf = tuple(torch.empty((Q, 3), device=device) for _ in range(3))
-    hout = torch.empty((Q, 3), dtype=torch.float32).pin_memory()
-    for i in range(args.warmup):
-        for dst, src in zip(dbuf, pinned[i % n_batches]):
-            dst.copy_(src, non_blocking=True)
-        rgb = train_step(grid, *dbuf)
-        hout.copy_(rgb, non_blocking=True)
+    dbuf = [tuple(torch.empty((Q, 3), device=device) for _ in range(3)) for _ in range(2)]
+    hout = [torch.empty((Q, 3), dtype=torch.float32).pin_memory() for _ in range(2)]
+    main = torch.cuda.current_stream(device)
+    copy = torch.cuda.Stream(device=device)
+    ev_in = [torch.cuda.Event() for _ in range(2)]      # inputs of a buffer have landed
+    ev_free = [torch.cuda.Event() for _ in range(2)]    # the step using a buffer has finished
+    ev_out = [torch.cuda.Event() for _ in range(2)]     # colours of a step are on the host
+
+    def upload(i):
+        k = i % 2
+        with torch.cuda.stream(copy):
+            copy.wait_event(ev_free[k])
+            for dst, src in zip(dbuf[k], pinned[i % n_batches]):
+                dst.copy_(src, non_blocking=True)
+            ev_in[k].record(copy)
+
+    def run(n):
+        upload(0)
+        for i in range(n):
+            k = i % 2
+            main.wait_event(ev_in[k])
+            if i + 1 < n:
+                upload(i + 1)
+            rgb = train_step(grid, *dbuf[k])
+            ev_free[k].record(main)
+            with torch.cuda.stream(copy):
+                copy.wait_event(ev_free[k])
+                hout[k].copy_(rgb, non_blocking=True)
+                rgb.record_stream(copy)
+                ev_out[k].record(copy)
+        main.wait_event(ev_out[(n - 1) % 2])          # the last read-back ends the job
+
+    run(args.warmup)
     torch.cuda.synchronize()
     if dist is not None:
         dist.barrier()
     e_start, e_stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e_start.record()
-    for i in range(args.steps):
-        for dst, src in zip(dbuf, pinned[i % n_batches]):
-            dst.copy_(src, non_blocking=True)
-        rgb = train_step(grid, *dbuf)
-        hout.copy_(rgb, non_blocking=True)
-    e_stop.record()
+    e_start.record(main)
+    run(args.steps)
+    e_stop.record(main)
     torch.cuda.synchronize()
     e2e_ms = e_start.elapsed_time(e_stop)
     e2e_ms = max_over_ranks(e2e_ms, dist, device)

@@ -337,6 +337,57 @@ def run_mixed(args):
     print(json.dumps(line), flush=True)
 
 
+def run_render(args):
+    """Forward-only render of the 256^3 workload (what a render request runs): args.rays rays
+    per step through the grid API (no gradient), SH stored FP32 and BF16.  Reports rays/s and the
+    forward kernel's roofline: 928 B (FP32) or 496 B (BF16) per evaluated sample + 24 B per ray."""
+    from svox2_gb300 import Rays, SparseGrid
+    from svox2_gb300 import synthetic as S
+    from svox2_gb300 import csrc as C
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    q = args.rays
+    g = S.make_grid(RESO, occupancy=OCC, n_balls=N_BALLS, seed=0, device=dev)
+    o, d, _ = [t.to(dev) for t in S.make_rays(q, seed=1000)]
+    peak, peak_kind = _peaks()
+    res = {}
+    for name, dt, per_sample in (("fp32", torch.float32, 928), ("bf16", torch.bfloat16, 496)):
+        grid = SparseGrid.from_tables(g.links.to(dev), g.density.to(dev), g.sh.to(dev).to(dt))
+        grid.opt.sigma_thresh, grid.opt.stop_thresh = 1e-8, 1e-7
+        spec, optc = grid._to_cpp(), grid.opt._to_cpp()
+        rays = C.RaysSpec()
+        rays.origins, rays.dirs = o, d
+        with torch.no_grad():
+            for _ in range(args.warmup):
+                grid.volume_render(Rays(o, d))
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(args.steps):
+                grid.volume_render(Rays(o, d))
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / args.steps
+            # the march kernel alone, with its evaluated-sample count
+            st = {"eval_samples": torch.zeros(1, dtype=torch.int64, device=dev),
+                  "march_start": torch.cuda.Event(enable_timing=True),
+                  "march_stop": torch.cuda.Event(enable_timing=True)}
+            C.volume_render_cuvol(spec, rays, optc, stats=st)
+            torch.cuda.synchronize()
+        kms = st["march_start"].elapsed_time(st["march_stop"])
+        n_eval = int(st["eval_samples"].item())
+        achieved = (n_eval * per_sample + 24 * q) / (kms / 1e3) / 1e9
+        res[name] = {"rays_per_s": q / (ms / 1e3), "ms_per_step": ms, "kernel_ms": kms, "eval_samples": n_eval,
+                     "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                                  "frac": achieved / peak, "peak_kind": peak_kind}}
+        del grid
+    line = {"metric": "forward render rays/s at 256^3 SH9 (render_kernel fwd), FP32 and BF16 SH storage",
+            "unit": "rays/s", "value": res["fp32"]["rays_per_s"], "steps": args.steps, "data": "synthetic",
+            "config": {"workload": f"256^3 20% occupancy SH9, {q} rays per step, no gradient"}, "results": res}
+    print(json.dumps(line), flush=True)
+
+
 def run_serve(args):
     """Serving configuration: a Poisson stream (2000 requests/s) of render requests (square
     images, side U{64..800}, cameras on a radius-4 sphere looking at the origin) and train-step
@@ -452,9 +503,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--rays", type=int, default=1_000_000, help="rays per step (profiling runs use a smaller case)")
     ap.add_argument("--skip-e2e", action="store_true", help="leave out the host-copy arm (profiling runs)")
-    ap.add_argument("--config", default="train", choices=["train", "mixed", "serve"],
+    ap.add_argument("--config", default="train", choices=["train", "mixed", "serve", "render"],
                     help="train: the 256^3 training step (default); mixed: 512^3 BF16/FP16 SH vs FP32; "
-                         "serve: continuous-batching server vs serial launches")
+                         "serve: continuous-batching server vs serial launches; "
+                         "render: forward-only render of the 256^3 workload, FP32 and BF16 SH")
     ap.add_argument("--requests", type=int, default=600, help="serve: number of requests in the stream")
     ap.add_argument("--rate", type=float, default=2000.0, help="serve: Poisson arrival rate (requests/s)")
     args = ap.parse_args()
@@ -463,6 +515,9 @@ def main():
         return
     if args.config == "serve":
         run_serve(args)
+        return
+    if args.config == "render":
+        run_render(args)
         return
     Q = args.rays
     args.warmup = max(args.warmup, 3)

@@ -234,8 +234,12 @@ __device__ __forceinline__ void camera_ray(int ix, int iy, const IoP& io, float 
 }
 
 // compute_skip_dist, render_util.cuh:235-295 (pos_offset = 0).
-__device__ __forceinline__ float skip_dist(int32_t link, const int l[3], const float pos[3],
-                                           const float d[3]) {
+// Out of line with scalar arguments: only accelerated grids take this path, and keeping it out
+// of the march's three inlined copies shortens the fused kernel.
+__device__ __noinline__ float skip_dist(int32_t link, int l0, int l1, int l2, float p0, float p1, float p2,
+                                        float d0, float d1, float d2) {
+  const int l[3] = {l0, l1, l2};
+  const float pos[3] = {p0, p1, p2}, d[3] = {d0, d1, d2};
   const uint32_t dist = (uint32_t)(-link);
   const uint32_t shift = dist - 1u;
   const uint32_t side = (uint32_t)((float)(1u << shift) - 1.f);
@@ -381,7 +385,8 @@ __device__ __forceinline__ void march_segment(Seg& s, float t0, float lt0, const
     for (int j = 0; j < 8; ++j) lk[j] = -1;
   }
   float skip = 0.f;
-  if (valid && lk[0] < -1) skip = skip_dist(lk[0], s.l, s.pos, r.d);
+  if (valid && lk[0] < -1)
+    skip = skip_dist(lk[0], s.l[0], s.l[1], s.l[2], s.pos[0], s.pos[1], s.pos[2], r.d[0], r.d[1], r.d[2]);
   const bool is_skip = valid && skip >= opt.step;
   const unsigned cut = __ballot_sync(kFull, !valid || is_skip);
   s.n = cut ? __ffs(cut) - 1 : 32;

@@ -541,7 +541,6 @@ def main():
 
     device = torch.device("cuda", local)
     torch.cuda.set_device(device)
-    import __graft_entry__ as ge  # noqa: F401  (path setup)
     from svox2_gb300 import Rays
 
     n_batches = min(args.steps + args.warmup, 8)

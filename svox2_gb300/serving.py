@@ -30,9 +30,7 @@ executor; ``RenderServer`` executes its plans on the GPU.
 from __future__ import annotations
 
 import ctypes as C
-import heapq
 import itertools
-import math
 import time
 from dataclasses import dataclass, field
 from typing import Callable, Dict, List, Optional, Tuple

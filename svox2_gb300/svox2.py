@@ -24,7 +24,7 @@ from torch import autograd, nn
 
 from . import csrc as _C
 from . import utils
-from .defs import BASIS_TYPE_3D_TEXTURE, BASIS_TYPE_MLP, BASIS_TYPE_SH
+from .defs import BASIS_TYPE_SH
 
 
 def _no_cpu_path(what: str):

@@ -37,7 +37,9 @@
 
 #include <climits>
 #include <cmath>
+#include <map>
 #include <mutex>
+#include <utility>
 
 namespace svx {
 namespace {
@@ -1296,14 +1298,16 @@ int launch_t(const GridP& g, const OptP& opt, IoP io, long long n_rays, cudaStre
   const int cap = MODE == kFwd ? 0 : io.cap;
   io.cap = cap;
   const size_t smem = sizeof(float) * (size_t)warp_smem_floats(C, cap, MODE != kFwd) * kWarps;
+  // per (device, colour-cache capacity): the shared-memory attribute is set on each device the
+  // kernel runs on, and the occupancy it allows is looked up once
   static std::mutex mu;
-  static int blocks_per_sm[2][1024];  // indexed by device, cap/4 (0 = unset)
+  static std::map<std::pair<int, int>, int> blocks_per_sm;
   int dev = 0;
   SVX_CUDA_TRY(cudaGetDevice(&dev));
   int bps;
   {
     std::lock_guard<std::mutex> lk(mu);
-    int& slot = blocks_per_sm[dev & 1][(cap / 4) & 1023];
+    int& slot = blocks_per_sm[std::make_pair(dev, cap)];
     if (slot == 0) {
       SVX_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       int b = 0;

@@ -48,9 +48,9 @@ Q = 1_000_000
 BYTES_PER_SAMPLE = 3648
 BYTES_PER_RAY = 48
 # DRAM bytes (read + write) per evaluated sample of render_kernel<9, float, fused> on this
-# workload: one ncu capture (--set full) of a 131,072-ray launch read 15.691 GB and wrote
-# 5.301 GB over 20,528,126 evaluated samples; scaled to a launch by its evaluated samples.
-DRAM_BYTES_PER_SAMPLE = 1022.6
+# workload: one ncu capture (--set full) of a 131,072-ray launch read 15.711 GB and wrote
+# 5.304 GB over 20,528,229 evaluated samples; scaled to a launch by its evaluated samples.
+DRAM_BYTES_PER_SAMPLE = 1023.7
 # launches of this library per training step: ray_keys_kernel, 6 CUB radix-sort kernels,
 # render_kernel, add_accum_kernel, 2 x tv_sparse_kernel, 2 x step_mask_kernel
 LAUNCHES_PER_STEP = 13

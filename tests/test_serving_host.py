@@ -123,3 +123,50 @@ def test_one_train_step_per_grid_per_batch():
     s.finish(ta1, 1.0)
     _, trains = s.plan()
     assert trains == [ta2]
+
+
+def test_grid_removal_waits_for_its_requests_and_memory_returns():
+    s = _sched()
+    s.add_grid("a", 4000)
+    base = s.used_bytes()
+    t = s.new_ticket("render", "a", 100, 1500, None, 0.0, None)
+    with pytest.raises(RuntimeError):
+        s.remove_grid("a")                    # a request is queued on it
+    assert s.admit() == [t]
+    assert s.used_bytes() == base + 1500      # the admitted request holds its buffers
+    s.plan()
+    s.finish(t, 1.0)
+    assert s.used_bytes() == base             # ... and returns them when it finishes
+    s.remove_grid("a")
+    assert s.used_bytes() == 0 and s.idle()
+
+
+def test_default_timeout_applies_and_failed_requests_unblock_their_grid():
+    s = _sched(default_timeout=0.5, max_inflight=1)
+    s.add_grid("a", 100)
+    r0 = s.new_ticket("render", "a", 10, 10, None, 0.0, None)
+    tr = s.new_ticket("train", "a", 10, 10, None, 0.1, None)
+    r1 = s.new_ticket("render", "a", 10, 10, None, 0.2, timeout=5.0)
+    assert s.admit() == [r0]                  # one slot: the others wait in the queue
+    expired = s.expire(0.7)                   # the train step's default 0.5 s deadline passed
+    assert expired == [tr] and tr.state == "failed"
+    assert r1.state == "queued"               # its own 5 s timeout still runs
+    s.plan()
+    s.finish(r0, 0.8)
+    assert s.admit() == [r1]
+    chunks, _ = s.plan()                      # the failed train step no longer orders r1
+    assert [c.ticket for c in chunks] == [r1]
+
+
+def test_train_step_waits_for_device_work_not_host_readback():
+    done = set()
+    s = _sched(work_done=lambda t: t.done or t.id in done)
+    s.add_grid("a", 100)
+    r = s.new_ticket("render", "a", 100, 10, None, 0.0, None)
+    tr = s.new_ticket("train", "a", 100, 10, None, 0.1, None)
+    s.admit()
+    chunks, trains = s.plan()
+    assert [c.ticket for c in chunks] == [r] and trains == []
+    done.add(r.id)                            # the render's kernels finished; its colours are still
+    _, trains = s.plan()                      # on their way to the host
+    assert trains == [tr]

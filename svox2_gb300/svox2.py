@@ -472,6 +472,24 @@ class SparseGrid(nn.Module):
                        ndc_coeffs[0], ndc_coeffs[1], grad)
             self.sparse_grad_indexer = None
 
+    def inplace_l2_color_grad(self, grad: torch.Tensor, start_dim: int = 0, end_dim: Optional[int] = None,
+                              scaling: float = 1.0):
+        """Add the gradient of an L2 penalty on the SH channels [start_dim, end_dim) into grad,
+        times scaling / (rows penalised): every row, or the rows of sparse_sh_grad_indexer
+        (svox2/svox2.py:1897-1932; plain tensor arithmetic, as in the reference)."""
+        with torch.no_grad():
+            C = self.sh_data.size(1)
+            end_dim = C if end_dim is None else (end_dim + C if end_dim < 0 else end_dim)
+            start_dim = start_dim + C if start_dim < 0 else start_dim
+            sh = self.sh_data[:, start_dim:end_dim].float()
+            if self.sparse_sh_grad_indexer is None:
+                grad[:, start_dim:end_dim] += (scaling / self.sh_data.size(0)) * sh
+            else:
+                idx = self.sparse_sh_grad_indexer
+                nz = int(torch.count_nonzero(idx).item()) if idx.dtype == torch.bool else idx.size(0)
+                if nz > 0:
+                    grad[idx, start_dim:end_dim] += (scaling / nz) * sh[idx]
+
     def inplace_tv_color_grad(self, grad: torch.Tensor, start_dim: int = 0, end_dim: Optional[int] = None,
                               scaling: float = 1.0, sparse_frac: float = 0.01, logalpha: bool = False,
                               logalpha_delta: float = 2.0, ndc_coeffs: Tuple[float, float] = (-1.0, -1.0),
@@ -769,4 +787,4 @@ class SparseGrid(nn.Module):
 
     sparsify_background = resize = to_svox1 = _unbuilt
     inplace_tv_lumisphere_grad = inplace_tv_background_grad = inplace_tv_basis_grad = _unbuilt
-    inplace_l2_color_grad = optim_background_step = optim_basis_step = _unbuilt
+    optim_background_step = optim_basis_step = _unbuilt

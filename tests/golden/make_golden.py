@@ -10,6 +10,7 @@ records inputs and outputs of
   * SparseGrid.sample(use_kernel=False) + autograd (svox2/svox2.py:576-653),
   * SparseGrid.save / SparseGrid.load of a checkpoint (svox2/svox2.py:1526-1628),
   * SparseGrid.resample on the CPU path without dilation (svox2/svox2.py:1223-1424),
+  * SparseGrid.inplace_l2_color_grad (svox2/svox2.py:1897-1932),
 into tests/golden/*.npz.  sigma_thresh = stop_thresh = 0 so that the CPU
 path's semantics coincide with the CUDA kernel's (the reference's own
 test/test_render_gradcheck.py uses the same setting).
@@ -143,6 +144,26 @@ def resample_case(svox2, name, reso, new_reso, occupancy, sigma_thresh, seed):
     print(name, "resampled voxels", grid.density_data.shape[0])
 
 
+def l2_case(svox2, name, seed):
+    """SparseGrid.inplace_l2_color_grad (svox2/svox2.py:1897-1932), dense and with a sparse
+    SH indexer, on the CPU (plain tensor arithmetic in the reference)."""
+    gen = torch.Generator().manual_seed(seed)
+    grid = svox2.SparseGrid(reso=6, basis_dim=9, device="cpu")
+    N = grid.sh_data.shape[0]
+    grid.sh_data.data[:] = torch.randn((N, 27), generator=gen)
+    g0 = torch.randn((N, 27), generator=gen)
+    dense = g0.clone()
+    grid.sparse_sh_grad_indexer = None
+    grid.inplace_l2_color_grad(dense, start_dim=3, end_dim=-2, scaling=0.7)
+    mask = torch.rand(N, generator=gen) < 0.05
+    sparse = g0.clone()
+    grid.sparse_sh_grad_indexer = mask
+    grid.inplace_l2_color_grad(sparse, scaling=1.3)
+    np.savez_compressed(OUT / f"l2_{name}.npz", sh=grid.sh_data.data.numpy(), grad0=g0.numpy(),
+                        mask=mask.numpy(), dense=dense.numpy(), sparse=sparse.numpy())
+    print(name, "l2 rows", N, "masked", int(mask.sum()))
+
+
 def main(ref_root: str):
     sys.path.insert(0, ref_root)
     warnings.filterwarnings("ignore")
@@ -155,6 +176,7 @@ def main(ref_root: str):
     sample_case(svox2, "dense10_sh9", 10, 9, 300, 15)
     checkpoint_case(svox2, "sparse10x12x14_sh9", (10, 12, 14), 9, 0.4, [1.2, 0.8, 1.0], [0.1, -0.2, 0.3], 16)
     resample_case(svox2, "sparse12_to_9x14x11", 12, [9, 14, 11], 0.5, 4.0, 17)
+    l2_case(svox2, "dense6_sh9", 18)
 
 
 if __name__ == "__main__":

@@ -283,6 +283,14 @@ typedef struct {
   int32_t n_cols;
 } svx_table_t;
 
+/* tv (svox2/csrc/svox2.cpp:60, loss_kernel.cu:42-109, host 483-515).  Writes
+ * to the device float *out the TV value of channels [start_dim, end_dim): the mean
+ * over the (size0-1)(size1-1)(size2-1) cells of sqrt(1e-5 + |d * size/256|^2),
+ * summed over channels.  use_logalpha must be 0 (the reference rejects it too). */
+int svx_tv(const int32_t* links, const int32_t size[3], const svx_table_t* data, int32_t start_dim,
+           int32_t end_dim, int32_t use_logalpha, float logalpha_delta, int32_t ignore_edge,
+           float ndc_coeffx, float ndc_coeffy, float* out, void* stream);
+
 /* tv_grad (svox2/csrc/svox2.cpp:62-63, loss_kernel.cu:111-176, host 522-556).
  * Dense TV gradient over all (size0-1)(size1-1)(size2-1) cells, channels
  * [start_dim, end_dim), scaled by scale / n_cells, accumulated into grad

@@ -267,3 +267,13 @@ def grid_weight_render(data, cam: dict, step_size, stop_thresh, last_opaque, off
        C.c_float(stop_thresh), C.c_int(int(last_opaque)), (C.c_float * 3)(*offset), (C.c_float * 3)(*scaling),
        C.c_void_p(w.ctypes.data))
     return w
+
+
+def tv_value(links, data, start, end, ignore_edge, prec="f64"):
+    """tv: the TV value of channels [start, end) of the float32 table data [N, C]."""
+    links = np.ascontiguousarray(links, dtype=np.int32)
+    data = np.ascontiguousarray(data, dtype=np.float32)
+    fn = getattr(lib(), "oracle_tv_value_" + prec)
+    fn.restype = C.c_double if prec == "f64" else C.c_float
+    return float(fn(C.c_void_p(links.ctypes.data), (C.c_int * 3)(*links.shape), C.c_void_p(data.ctypes.data),
+                    C.c_int(data.shape[1]), C.c_int(start), C.c_int(end), C.c_int(int(ignore_edge))))

@@ -593,6 +593,37 @@ void FN(oracle_sample_backward)(const oracle_grid_t* g, const float* pts, int64_
   }
 }
 
+/* tv_kernel, svox2/csrc/loss_kernel.cu:42-109 (host 483-515): the TV value, the mean over
+ * cells of sqrt(1e-5 + |d * size/256|^2) summed over channels [start, end); a cell whose voxel
+ * has link 0 is skipped with ignore_edge (the reference's early return), and a missing
+ * neighbour reads 0 (or the voxel's own value with ignore_edge).  Summed in REAL. */
+REAL FN(oracle_tv_value)(const int32_t* links, const int size[3], const float* data, int ncols, int start,
+                         int end, int ignore_edge) {
+  const int64_t offy = size[2], offx = (int64_t)size[1] * size[2];
+  const REAL sx = (REAL)size[0] * (REAL)(1.f / 256.f), sy = (REAL)size[1] * (REAL)(1.f / 256.f),
+             sz = (REAL)size[2] * (REAL)(1.f / 256.f);
+  const int nl = (size[0] - 1) * (size[1] - 1) * (size[2] - 1);
+  REAL sum = 0;
+  int x, y, z, c;
+  for (x = 0; x < size[0] - 1; ++x)
+    for (y = 0; y < size[1] - 1; ++y)
+      for (z = 0; z < size[2] - 1; ++z) {
+        const int32_t* lp = links + x * offx + y * offy + z;
+        const int32_t l000 = lp[0], l100 = lp[offx], l010 = lp[offy], l001 = lp[1];
+        if (ignore_edge && l000 == 0) continue;
+        for (c = start; c < end; ++c) {
+          const REAL v000 = l000 >= 0 ? (REAL)data[(int64_t)l000 * ncols + c] : 0;
+          const REAL nul = ignore_edge ? v000 : 0;
+          const REAL v100 = l100 >= 0 ? (REAL)data[(int64_t)l100 * ncols + c] : nul;
+          const REAL v010 = l010 >= 0 ? (REAL)data[(int64_t)l010 * ncols + c] : nul;
+          const REAL v001 = l001 >= 0 ? (REAL)data[(int64_t)l001 * ncols + c] : nul;
+          const REAL dx = (v100 - v000) * sx, dy = (v010 - v000) * sy, dz = (v001 - v000) * sz;
+          sum = sum + SQRT((REAL)1e-5f + dx * dx + dy * dy + dz * dz);
+        }
+      }
+  return sum * ((REAL)1 / (REAL)nl);
+}
+
 /* tv_grad_sparse_kernel, svox2/csrc/loss_kernel.cu:178-246 (host 558-604), and
  * tv_grad_kernel 111-176 (host 522-556) when cells == NULL. */
 void FN(oracle_tv_grad)(const int32_t* links, const int size[3], const float* data, int64_t n_rows, int ncols,

@@ -117,6 +117,7 @@ SIGNATURES = {
     "svx_grid_weight_render": [_vp, P(_i32), P(SvxCamera), _f32, _f32, _i32, P(_f32), P(_f32), _vp, _vp],
     "svx_volume_render_expected_term": [P(SvxGrid), P(SvxRays), P(SvxRenderOpts), _vp, _vp],
     "svx_volume_render_sigma_thresh": [P(SvxGrid), P(SvxRays), P(SvxRenderOpts), _f32, _vp, _vp],
+    "svx_tv": [_vp, P(_i32), P(SvxTable), _i32, _i32, _i32, _f32, _i32, _f32, _f32, _vp, _vp],
     "svx_tv_grad": [_vp, P(_i32), P(SvxTable), _i32, _i32, _f32, _i32, _f32, _i32, _f32, _f32, _vp, _vp],
     "svx_tv_grad_sparse": [_vp, P(_i32), P(SvxTable), _vp, _i64, _vp, _i32, _i32, _f32, _i32, _f32, _i32,
                            _i32, _f32, _f32, _vp, _vp],

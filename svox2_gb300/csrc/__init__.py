@@ -28,7 +28,7 @@ __all__ = [
     "volume_render_cuvol", "volume_render_cuvol_image", "volume_render_cuvol_backward",
     "volume_render_cuvol_fused", "sample_grid", "sample_grid_backward", "tv_grad",
     "tv_grad_sparse", "rmsprop_step", "sgd_step", "accel_dist_prop", "volume_render_expected_term",
-    "volume_render_sigma_thresh", "dilate", "grid_weight_render",
+    "volume_render_sigma_thresh", "dilate", "grid_weight_render", "tv",
 ]
 
 _DTYPES = {torch.float32: _lib.SVX_F32, torch.bfloat16: _lib.SVX_BF16, torch.float16: _lib.SVX_F16}
@@ -401,6 +401,20 @@ def grid_weight_render(data: torch.Tensor, cam: CameraSpec, step_size: float, st
         _lib.call("svx_grid_weight_render", d.data_ptr(), (C.c_int32 * 3)(*d.shape), C.byref(c), float(step_size),
                   float(stop_thresh), int(bool(last_sample_opaque)), (C.c_float * 3)(*off), (C.c_float * 3)(*scl),
                   w.data_ptr(), _stream(d.device))
+
+
+def tv(links: torch.Tensor, data: torch.Tensor, start_dim: int, end_dim: int, use_logalpha: bool,
+       logalpha_delta: float, ignore_edge: bool, ndc_coeffx: float, ndc_coeffy: float) -> torch.Tensor:
+    """svox2/csrc/loss_kernel.cu:483-515: the TV value (a 0-d float32 tensor on the data's device)."""
+    lt, size = _links_args(links)
+    tab = _table(data, "data")
+    dev = data.device
+    out = torch.empty((), dtype=torch.float32, device=dev)
+    with torch.cuda.device(dev):
+        _lib.call("svx_tv", lt.data_ptr(), size, C.byref(tab), int(start_dim), int(end_dim), int(bool(use_logalpha)),
+                  float(logalpha_delta), int(bool(ignore_edge)), float(ndc_coeffx), float(ndc_coeffy),
+                  out.data_ptr(), _stream(dev))
+    return out
 
 
 def tv_grad(links: torch.Tensor, data: torch.Tensor, start_dim: int, end_dim: int, scale: float,

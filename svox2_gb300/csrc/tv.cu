@@ -1,6 +1,6 @@
-// Total-variation gradients on the voxel grid.
+// Total variation on the voxel grid: its value and its gradients.
 //
-// Replaces svox2/csrc/loss_kernel.cu: tv_grad_kernel 111-176 (dense over all
+// Replaces svox2/csrc/loss_kernel.cu: tv_kernel 42-109 (the value), tv_grad_kernel 111-176 (dense over all
 // cells) and tv_grad_sparse_kernel 178-246 (a list of cells, the training
 // default), with their host launchers 522-604.  One thread per (cell, channel),
 // channels innermost so that a warp reads consecutive coefficients of the same
@@ -117,6 +117,52 @@ __global__ void __launch_bounds__(256) tv_dense_kernel(TvArgs a) {
   }
 }
 
+// The TV value (tv_kernel, loss_kernel.cu:42-109): the mean over cells of
+// sqrt(1e-5 + |d ⊙ size/256|^2), summed over channels, d the forward differences of
+// the cell's voxel to its +x/+y/+z neighbours (missing neighbour: 0, or the voxel's own
+// value with ignore_edge; a cell whose voxel has link 0 is skipped with ignore_edge).
+// Each block sums its terms in shared memory and adds the block's sum with one atomic;
+// out (a device float, zeroed by the host) receives sum * scale.
+template <typename T>
+__global__ void __launch_bounds__(256) tv_value_kernel(TvArgs a, float* __restrict__ out) {
+  __shared__ float part[8];
+  const long long ncell = (long long)(a.X - 1) * (a.Y - 1) * (a.Z - 1);
+  const long long total = ncell * a.nch;
+  const float sx = a.X * (1.f / 256.f), sy = a.Y * (1.f / 256.f), sz = a.Z * (1.f / 256.f);
+  float acc = 0.f;
+  for (long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x; tid < total;
+       tid += (long long)gridDim.x * blockDim.x) {
+    const int idx = (int)(tid % a.nch) + a.start;
+    const long long xyz = tid / a.nch;
+    const int z = (int)(xyz % (a.Z - 1));
+    const long long xy = xyz / (a.Z - 1);
+    const int y = (int)(xy % (a.Y - 1)), x = (int)(xy / (a.Y - 1));
+    const long long offy = a.Z, offx = (long long)a.Y * a.Z;
+    const int32_t* lp = a.links + x * offx + y * offy + z;
+    const int l000 = __ldg(lp);
+    if (a.ignore_edge && l000 == 0) continue;
+    const int l100 = __ldg(lp + offx), l010 = __ldg(lp + offy), l001 = __ldg(lp + 1);
+    const float v000 = l000 >= 0 ? rd<T>(a, l000, idx) : 0.f;
+    const float nul = a.ignore_edge ? v000 : 0.f;
+    const float v100 = l100 >= 0 ? rd<T>(a, l100, idx) : nul;
+    const float v010 = l010 >= 0 ? rd<T>(a, l010, idx) : nul;
+    const float v001 = l001 >= 0 ? rd<T>(a, l001, idx) : nul;
+    const float dx = __fmul_rn(__fsub_rn(v100, v000), sx);
+    const float dy = __fmul_rn(__fsub_rn(v010, v000), sy);
+    const float dz = __fmul_rn(__fsub_rn(v001, v000), sz);
+    acc = __fadd_rn(acc, sqrtf(fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, 1e-5f)))));
+  }
+#pragma unroll
+  for (int d = 16; d >= 1; d >>= 1) acc = __fadd_rn(acc, __shfl_xor_sync(0xffffffffu, acc, d));
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float b = 0.f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) b = __fadd_rn(b, part[w]);
+    atomicAdd(out, __fmul_rn(b, a.scale));
+  }
+}
+
 int make_tv(const int32_t* links, const int32_t size[3], const svx_table_t* data, int start, int end,
             float* grad, TvArgs* a) {
   SVX_REQUIRE(links && size && data && data->data && grad, SVX_ERR_INVALID, "null argument");
@@ -208,5 +254,33 @@ extern "C" int svx_tv_grad_sparse(const int32_t* links, const int32_t size[3], c
     default: tv_sparse_kernel<__half><<<blocks, 256, 0, st>>>(a, rand_cells, n_cells);
   }
   SVX_LAUNCH_CHECK("tv_sparse_kernel");
+  return SVX_OK;
+}
+
+extern "C" int svx_tv(const int32_t* links, const int32_t size[3], const svx_table_t* data, int32_t start_dim,
+                      int32_t end_dim, int32_t use_logalpha, float logalpha_delta, int32_t ignore_edge,
+                      float ndc_coeffx, float ndc_coeffy, float* out, void* stream) {
+  (void)logalpha_delta;
+  (void)ndc_coeffx;
+  (void)ndc_coeffy;
+  clear_error();
+  SVX_REQUIRE(!use_logalpha, SVX_ERR_UNSUPPORTED, "use_logalpha is no longer supported (as in the reference)");
+  SVX_REQUIRE(out != nullptr, SVX_ERR_INVALID, "out is null");
+  TvArgs a;
+  int rc = make_tv(links, size, data, start_dim, end_dim, out, &a);
+  if (rc) return rc;
+  const long long ncell = (long long)(a.X - 1) * (a.Y - 1) * (a.Z - 1);
+  a.scale = 1.f / (float)(int)ncell;
+  a.ignore_edge = ignore_edge != 0;
+  a.ignore_last_z = 0;
+  cudaStream_t st = as_stream(stream);
+  SVX_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(float), st));
+  const unsigned blocks = grid_for(ncell * a.nch);
+  switch (data->dtype) {
+    case SVX_F32: tv_value_kernel<float><<<blocks, 256, 0, st>>>(a, out); break;
+    case SVX_BF16: tv_value_kernel<__nv_bfloat16><<<blocks, 256, 0, st>>>(a, out); break;
+    default: tv_value_kernel<__half><<<blocks, 256, 0, st>>>(a, out);
+  }
+  SVX_LAUNCH_CHECK("tv_value_kernel");
   return SVX_OK;
 }

@@ -194,6 +194,33 @@ class _SampleGridAutogradFunction(autograd.Function):
         return grad_density_grid, grad_sh_grid, None, None, None
 
 
+class _TotalVariationFunction(autograd.Function):
+    """TV value of channels [start_dim, end_dim) of a grid table and its gradient
+    (svox2/svox2.py:292-329): forward tv, backward tv_grad.  The reference returns the
+    gradient of the TV itself whatever the incoming gradient; here it is scaled by it, as
+    autograd expects (identical for a TV term used with weight 1)."""
+
+    @staticmethod
+    def forward(ctx, data, links, start_dim, end_dim, use_logalpha, logalpha_delta, ignore_edge, ndc_coeffs):
+        value = _C.tv(links, data, start_dim, end_dim, use_logalpha, logalpha_delta, ignore_edge,
+                      ndc_coeffs[0], ndc_coeffs[1])
+        ctx.save_for_backward(links, data)
+        ctx.args = (start_dim, end_dim, use_logalpha, logalpha_delta, ignore_edge, ndc_coeffs)
+        return value
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        links, data = ctx.saved_tensors
+        start_dim, end_dim, use_logalpha, logalpha_delta, ignore_edge, ndc_coeffs = ctx.args
+        grad = None
+        if ctx.needs_input_grad[0]:
+            grad = torch.zeros(data.shape, dtype=torch.float32, device=data.device)
+            _C.tv_grad(links, data, start_dim, end_dim, 1.0, use_logalpha, logalpha_delta, ignore_edge,
+                       ndc_coeffs[0], ndc_coeffs[1], grad)
+            grad = (grad * grad_out).to(data.dtype)
+        return grad, None, None, None, None, None, None, None
+
+
 class _VolumeRenderFunction(autograd.Function):
     """svox2/svox2.py:226-288.  The backward is the reverse-order adjoint kernel;
     the colour it is handed is not needed by it and is kept for interface parity."""
@@ -489,6 +516,29 @@ class SparseGrid(nn.Module):
                 nz = int(torch.count_nonzero(idx).item()) if idx.dtype == torch.bool else idx.size(0)
                 if nz > 0:
                     grad[idx, start_dim:end_dim] += (scaling / nz) * sh[idx]
+
+    def tv(self, logalpha: bool = False, logalpha_delta: float = 2.0,
+           ndc_coeffs: Tuple[float, float] = (-1.0, -1.0)):
+        """Total variation of the density, a differentiable scalar: the sum over channels of the
+        mean over cells (svox2/svox2.py:1678-1693)."""
+        if not self.links.is_cuda:
+            _no_cpu_path("SparseGrid.tv")
+        assert not logalpha, "No longer supported"
+        return _TotalVariationFunction.apply(self.density_data, self.links, 0, 1, logalpha, logalpha_delta,
+                                             False, ndc_coeffs)
+
+    def tv_color(self, start_dim: int = 0, end_dim: Optional[int] = None, logalpha: bool = False,
+                 logalpha_delta: float = 2.0, ndc_coeffs: Tuple[float, float] = (-1.0, -1.0)):
+        """Total variation of the SH channels [start_dim, end_dim), a differentiable scalar
+        (svox2/svox2.py:1695-1722)."""
+        if not self.links.is_cuda:
+            _no_cpu_path("SparseGrid.tv_color")
+        assert not logalpha, "No longer supported"
+        C = self.sh_data.size(1)
+        end_dim = C if end_dim is None else (end_dim + C if end_dim < 0 else end_dim)
+        start_dim = start_dim + C if start_dim < 0 else start_dim
+        return _TotalVariationFunction.apply(self.sh_data, self.links, start_dim, end_dim, logalpha,
+                                             logalpha_delta, True, ndc_coeffs)
 
     def inplace_tv_color_grad(self, grad: torch.Tensor, start_dim: int = 0, end_dim: Optional[int] = None,
                               scaling: float = 1.0, sparse_frac: float = 0.01, logalpha: bool = False,

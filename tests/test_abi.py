@@ -41,3 +41,32 @@ def test_errors_are_reported_without_a_gpu():
     assert b"null" in lib.svx_last_error()
     rc = lib.svx_rmsprop_step(None, 0, None, None, 10, 3, 9, None, 0, 0.9, 1.0, 1e-8, -1e9, -1.0, None)
     assert rc == _lib.SVX_ERR_INVALID
+
+
+def test_new_entry_points_validate_on_the_host():
+    """Null or out-of-range arguments of every entry point beyond the reference's first table
+    return a status and a message before any CUDA call."""
+    import ctypes as C
+    from svox2_gb300 import _lib
+    lib = _lib.load()
+    size = (C.c_int32 * 3)(4, 4, 4)
+    cases = [
+        (lambda: lib.svx_accel_dist_prop(None, size, None), _lib.SVX_ERR_INVALID, b"null"),
+        (lambda: lib.svx_accel_dist_prop(None, None, None), _lib.SVX_ERR_INVALID, b"null"),
+        (lambda: lib.svx_dilate(None, None, size, None), _lib.SVX_ERR_INVALID, b"null"),
+        (lambda: lib.svx_tv(None, size, None, 0, 1, 1, C.c_float(2.0), 0, C.c_float(-1.0), C.c_float(-1.0), None,
+                            None), _lib.SVX_ERR_UNSUPPORTED, b"logalpha"),
+        (lambda: lib.svx_tv(None, size, None, 0, 1, 0, C.c_float(2.0), 0, C.c_float(-1.0), C.c_float(-1.0), None,
+                            None), _lib.SVX_ERR_INVALID, b"null"),
+        (lambda: lib.svx_add_accum(None, 26, 27, 10, None, None, None), _lib.SVX_ERR_INVALID, b"stride"),
+        (lambda: lib.svx_ray_order(None, None, None, 0, None, None), _lib.SVX_ERR_INVALID, b"null"),
+        (lambda: lib.svx_volume_render_expected_term(None, None, None, None, None), _lib.SVX_ERR_INVALID, b"null"),
+        (lambda: lib.svx_volume_render_sigma_thresh(None, None, None, C.c_float(1.0), None, None),
+         _lib.SVX_ERR_INVALID, b"null"),
+        (lambda: lib.svx_grid_weight_render(None, size, None, C.c_float(0.5), C.c_float(0.0), 0, None, None, None,
+                                            None), _lib.SVX_ERR_INVALID, b"null"),
+        (lambda: lib.svx_camera_rays(None, None, None, None), _lib.SVX_ERR_INVALID, b"null"),
+    ]
+    for call, status, word in cases:
+        assert call() == status, lib.svx_last_error()
+        assert word in lib.svx_last_error()

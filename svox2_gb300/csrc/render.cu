@@ -1525,8 +1525,11 @@ static int render_rays(const svx_grid_t* grid, const svx_rays_t* rays, const svx
   const bool grads = MODE != kFwd && (io.grad_sh != nullptr || io.grad_density != nullptr);
   const int C = grid->sh_data_dim;
   const int stride = (C + 1 + 3) & ~3;
-  if (grads) {
-    // gradient rows padded to 16 bytes, accumulated with vector atomics, then added once
+  // large batches accumulate into gradient rows padded to 16 bytes with vector atomics, added
+  // once at the end; small ones add straight into the gradients with scalar atomics (clearing
+  // and adding a table the size of the grid would cost more than the atomics it saves)
+  const bool table = grads && rays->n_rays >= kSortMinRays;
+  if (table) {
     const size_t bytes = sizeof(float) * (size_t)stride * (size_t)grid->n_voxels;
     rc = scr.alloc(1, bytes > 0 ? bytes : 16);
     if (rc) return rc;
@@ -1547,7 +1550,7 @@ static int render_rays(const svx_grid_t* grid, const svx_rays_t* rays, const svx
   if (rc) return rc;
   rc = mark(stats, true, st);
   if (rc) return rc;
-  if (grads) return launch_add_accum(io.accum, stride, C, grid->n_voxels, io.grad_sh, io.grad_density, st);
+  if (table) return launch_add_accum(io.accum, stride, C, grid->n_voxels, io.grad_sh, io.grad_density, st);
   return SVX_OK;
 }
 

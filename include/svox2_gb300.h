@@ -34,7 +34,7 @@ extern "C" {
 typedef enum {
   SVX_OK = 0,
   SVX_ERR_INVALID = 1,      /* bad argument: null pointer, size, dtype, range */
-  SVX_ERR_UNSUPPORTED = 2,  /* feature this library does not implement (MSI background, MLP basis…) */
+  SVX_ERR_UNSUPPORTED = 2,  /* feature this library does not implement (MLP basis, 3D texture…) */
   SVX_ERR_CUDA = 3,         /* a CUDA runtime call or kernel launch failed */
   SVX_ERR_TOO_LARGE = 4     /* size beyond a documented limit */
 } svx_status;
@@ -57,7 +57,16 @@ typedef enum { SVX_F32 = 0, SVX_BF16 = 1, SVX_F16 = 2 } svx_dtype;
  *              coefficient k of colour channel c is sh[v, c*basis_dim + k].
  *   offset/scaling  world -> grid transform, grid = world*scaling + offset
  *              (the reference's _offset/_scaling CPU tensors, svox2/svox2.py:2135-2161).
- *   background_nlayers  must be 0 (the MSI background model is not built). */
+ *   background_nlayers  0, or the layer count (>= 2) of the MSI background model
+ *              (svox2/svox2.py:497-521), whose tables are:
+ *   background_links  int32 [2 * background_reso, background_reso], C-contiguous;
+ *              >= 0 is a row of background_data, < 0 is empty.
+ *   background_data   float32 [background_capacity, background_nlayers, 4], 16-byte
+ *              aligned: per layer three colour coefficients (scaled by the SH DC
+ *              constant) and sigma.  A link >= background_capacity reads as empty.
+ * The MSI background is rendered by the ray entry points (cuvol.cu:386-607);
+ * svx_render_batch, svx_ray_order and the depth renders ignore it, as the
+ * reference's depth renders do. */
 typedef struct {
   const float* density_data;
   const void* sh_data;
@@ -71,6 +80,10 @@ typedef struct {
   int32_t background_nlayers;
   float offset[3];
   float scaling[3];
+  const int32_t* background_links;
+  const float* background_data;
+  int64_t background_capacity;
+  int32_t background_reso;
 } svx_grid_t;
 
 /* RaysSpec, data_spec.hpp:104-113: origins and unit directions, float32 [n_rays, 3]. */
@@ -103,11 +116,16 @@ typedef struct {
 
 /* GridOutputGrads, data_spec.hpp:54-81.  Gradients are float32 and are
  * ACCUMULATED into (not overwritten).  mask_out (bool/uint8 [n_voxels]) may be
- * NULL; when given, every voxel that received a gradient is set to 1. */
+ * NULL; when given, every voxel that received a gradient is set to 1.
+ * grad_background_out (float32 [capacity, nlayers, 4]) and mask_background_out
+ * (bool/uint8 [capacity, nlayers]) are the MSI background's, used when the grid
+ * has one; either may be NULL. */
 typedef struct {
   float* grad_density_out;
   float* grad_sh_out;
   uint8_t* mask_out;
+  float* grad_background_out;
+  uint8_t* mask_background_out;
 } svx_grid_grads_t;
 
 /* Optional instrumentation for the render entry points (may be NULL):
@@ -310,6 +328,19 @@ int svx_tv_grad_sparse(const int32_t* links, const int32_t size[3], const svx_ta
                        int32_t start_dim, int32_t end_dim, float scale, int32_t use_logalpha,
                        float logalpha_delta, int32_t ignore_edge, int32_t ignore_last_z,
                        float ndc_coeffx, float ndc_coeffy, float* grad, void* stream);
+
+/* msi_tv_grad_sparse (svox2/csrc/svox2.cpp:66, loss_kernel.cu:248-333, host 606-641).
+ * TV gradient of the MSI background on the n_cells cell indices rand_cells
+ * (int32, index = (x * reso + y) * nlayers + z over the [2 reso, reso, nlayers]
+ * cells): differences to the next cell in x and y wrap around, in z they stop
+ * at the last layer.  Channels 0..n_channels-2 are scaled by scale / n_cells,
+ * the last (sigma) by scale_last / n_cells.  links int32 [2 reso, reso] (a link
+ * >= capacity reads as empty); msi and grad float32 [capacity, nlayers,
+ * n_channels]; mask_out (uint8 [capacity, nlayers]) may be NULL.  Cell indices
+ * outside the MSI are skipped. */
+int svx_msi_tv_grad_sparse(const int32_t* links, int32_t reso, const float* msi, int64_t capacity,
+                           int32_t nlayers, int32_t n_channels, const int32_t* rand_cells, int64_t n_cells,
+                           uint8_t* mask_out, float scale, float scale_last, float* grad, void* stream);
 
 /* ---- optimisers: svox2/csrc/optim_kernel.cu ---------------------------- */
 

@@ -23,12 +23,13 @@ _lib = None
 class OGrid(C.Structure):
     _fields_ = [("links", C.c_void_p), ("density", C.c_void_p), ("sh", C.c_void_p), ("n_voxels", C.c_int64),
                 ("size", C.c_int * 3), ("basis_dim", C.c_int), ("offset", C.c_float * 3),
-                ("scaling", C.c_float * 3)]
+                ("scaling", C.c_float * 3), ("bg_links", C.c_void_p), ("bg_data", C.c_void_p), ("bg_reso", C.c_int),
+                ("bg_nlayers", C.c_int)]
 
 
 class OOpt(C.Structure):
     _fields_ = [("bg", C.c_float), ("step", C.c_float), ("sigma_thresh", C.c_float), ("stop_thresh", C.c_float),
-                ("near_clip", C.c_float), ("spheric", C.c_int), ("last_opaque", C.c_int)]
+                ("near_clip", C.c_float), ("spheric", C.c_int), ("last_opaque", C.c_int), ("bg_cpu", C.c_int)]
 
 
 class OCam(C.Structure):
@@ -52,12 +53,22 @@ class Grid:
     basis_dim: int
     offset: tuple              # grid = world * scaling + offset (the reference's _to_cpp transform)
     scaling: tuple
+    bg_links: Optional[np.ndarray] = None   # int32 [2 * reso, reso]: MSI background (None: none)
+    bg_data: Optional[np.ndarray] = None    # float32 [capacity, nlayers, 4]
 
     def struct(self) -> OGrid:
         self.links = np.ascontiguousarray(self.links, dtype=np.int32)
         self.density = np.ascontiguousarray(self.density, dtype=np.float32)
         self.sh = np.ascontiguousarray(self.sh, dtype=np.float32)
         g = OGrid()
+        if self.bg_links is not None and self.bg_links.size > 0:
+            self.bg_links = np.ascontiguousarray(self.bg_links, dtype=np.int32)
+            self.bg_data = np.ascontiguousarray(self.bg_data, dtype=np.float32)
+            assert self.bg_data.ndim == 3 and self.bg_data.shape[2] == 4 and self.bg_data.shape[1] >= 2
+            g.bg_links = self.bg_links.ctypes.data
+            g.bg_data = self.bg_data.ctypes.data
+            g.bg_reso = self.bg_links.shape[1]
+            g.bg_nlayers = self.bg_data.shape[1]
         g.links = self.links.ctypes.data
         g.density = self.density.ctypes.data
         g.sh = self.sh.ctypes.data
@@ -78,10 +89,12 @@ class Opt:
     near_clip: float = 0.0
     use_spheric_clip: bool = False
     last_sample_opaque: bool = False
+    bg_cpu_semantics: bool = False   # MSI background as the reference's pure-PyTorch path computes it
 
     def struct(self) -> OOpt:
         return OOpt(self.background_brightness, self.step_size, self.sigma_thresh, self.stop_thresh,
-                    self.near_clip, int(self.use_spheric_clip), int(self.last_sample_opaque))
+                    self.near_clip, int(self.use_spheric_clip), int(self.last_sample_opaque),
+                    int(self.bg_cpu_semantics))
 
 
 def _real(prec: str):
@@ -101,7 +114,9 @@ def default_threads() -> int:
 def render(grid: Grid, opt: Opt, origins, dirs, mode: int = 0, rgb_gt=None, grad_out=None, color=None,
            beta_loss: float = 0.0, sparsity_loss: float = 0.0, prec: str = "f32", want_grads: bool = True,
            want_mask: bool = True, trace: bool = False, nthreads: Optional[int] = None) -> dict:
-    """volume_render_cuvol (mode 0), _fused (1), _backward (2, color = forward colour)."""
+    """volume_render_cuvol (mode 0), _fused (1), _backward (2, color = forward colour).
+    With an MSI background the result also holds grad_background [capacity, nlayers, 4] and,
+    in mode 1, mask_background [capacity, nlayers]."""
     R = _real(prec)
     origins = np.ascontiguousarray(origins, dtype=np.float32)
     dirs = np.ascontiguousarray(dirs, dtype=np.float32)
@@ -114,6 +129,9 @@ def render(grid: Grid, opt: Opt, origins, dirs, mode: int = 0, rgb_gt=None, grad
     mask = np.zeros((N,), dtype=np.uint8) if (mode == 1 and want_mask) else None
     tr = np.zeros((Q,), dtype=np.uint64) if trace else None
     ne = np.zeros((1,), dtype=np.uint64)
+    has_bg = grid.bg_links is not None and grid.bg_links.size > 0
+    gbg = np.zeros(grid.bg_data.shape, dtype=R) if (has_bg and mode and want_grads) else None
+    mbg = np.zeros(grid.bg_data.shape[:2], dtype=np.uint8) if (has_bg and mode == 1 and want_mask) else None
     gt = None if rgb_gt is None else np.ascontiguousarray(rgb_gt, dtype=np.float32)
     go = None if grad_out is None else np.ascontiguousarray(grad_out, dtype=np.float32)
     g = grid.struct()
@@ -122,9 +140,10 @@ def render(grid: Grid, opt: Opt, origins, dirs, mode: int = 0, rgb_gt=None, grad
     fn.restype = None
     fn(C.byref(g), C.byref(o), C.c_void_p(_p(origins)), C.c_void_p(_p(dirs)), C.c_int64(Q), C.c_int(mode),
        C.c_void_p(_p(gt)), C.c_void_p(_p(go)), C.c_float(beta_loss), C.c_float(sparsity_loss),
-       C.c_void_p(_p(rgb)), C.c_void_p(_p(gd)), C.c_void_p(_p(gs)), C.c_void_p(_p(mask)), C.c_void_p(_p(tr)),
-       C.c_void_p(_p(ne)), C.c_int(nthreads or default_threads()))
+       C.c_void_p(_p(rgb)), C.c_void_p(_p(gd)), C.c_void_p(_p(gs)), C.c_void_p(_p(mask)), C.c_void_p(_p(gbg)),
+       C.c_void_p(_p(mbg)), C.c_void_p(_p(tr)), C.c_void_p(_p(ne)), C.c_int(nthreads or default_threads()))
     return {"rgb": rgb, "grad_density": gd, "grad_sh": gs, "mask": None if mask is None else mask.astype(bool),
+            "grad_background": gbg, "mask_background": None if mbg is None else mbg.astype(bool),
             "trace": tr, "n_eval": int(ne[0])}
 
 
@@ -277,3 +296,19 @@ def tv_value(links, data, start, end, ignore_edge, prec="f64"):
     fn.restype = C.c_double if prec == "f64" else C.c_float
     return float(fn(C.c_void_p(links.ctypes.data), (C.c_int * 3)(*links.shape), C.c_void_p(data.ctypes.data),
                     C.c_int(data.shape[1]), C.c_int(start), C.c_int(end), C.c_int(int(ignore_edge))))
+
+
+def msi_tv_grad(links, msi, cells, scale, scale_last, grad=None, mask=None, prec="f32"):
+    """msi_tv_grad_sparse: adds the MSI background's TV gradient over the listed cells to
+    grad (float [capacity, nlayers, channels], returned) and sets mask [capacity, nlayers]."""
+    R = _real(prec)
+    links = np.ascontiguousarray(links, dtype=np.int32)
+    msi = np.ascontiguousarray(msi, dtype=np.float32)
+    cl = np.ascontiguousarray(cells, dtype=np.int32)
+    grad = np.zeros(msi.shape, dtype=R) if grad is None else grad
+    fn = getattr(lib(), "oracle_msi_tv_grad_" + prec)
+    fn.restype = None
+    fn(C.c_void_p(links.ctypes.data), C.c_int(links.shape[0]), C.c_int(links.shape[1]), C.c_void_p(msi.ctypes.data),
+       C.c_int(msi.shape[1]), C.c_int(msi.shape[2]), C.c_void_p(cl.ctypes.data), C.c_int64(cl.shape[0]),
+       C.c_float(scale), C.c_float(scale_last), C.c_void_p(grad.ctypes.data), C.c_void_p(_p(mask)))
+    return grad

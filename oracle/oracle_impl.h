@@ -232,7 +232,7 @@ static void FN(fwd_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const R
   FN(calc_sh)(g->basis_dim, dir, basis);
   FN(find_bounds)(&r, org, dir, g, opt);
   if (r.tmin > r.tmax) {
-    for (c = 0; c < 3; ++c) out[c] = (REAL)opt->bg;
+    for (c = 0; c < 3; ++c) out[c] = g->bg_nlayers == 0 ? (REAL)opt->bg : (REAL)0;
     *log_t = 0;
     if (trace) *trace = h;
     return;
@@ -270,31 +270,36 @@ static void FN(fwd_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const R
     }
     t = t + step;
   }
-  for (c = 0; c < 3; ++c) out[c] = outv[c] + EXP(lt) * (REAL)opt->bg;
+  /* with an MSI background the brightness term is added after it (cuvol.cu:111-113, 474) */
+  for (c = 0; c < 3; ++c) out[c] = g->bg_nlayers == 0 ? outv[c] + EXP(lt) * (REAL)opt->bg : outv[c];
   *log_t = lt;
   if (trace) *trace = h;
 }
 
 /* trace_ray_cuvol_backward, render_lerp_kernel_cuvol.cu:227-383, forward order:
- * accum starts at dot(colour, gout) and loses each sample's contribution. */
+ * accum starts at dot(colour, gout) and loses each sample's contribution.  Reports the
+ * accum left after the last sample (beta term taken out) and the log transmittance there,
+ * which the MSI background's backward starts from (cuvol.cu:253-258, 374-383). */
 static void FN(bwd_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const REAL org[3], const REAL dir[3],
                         const REAL color[3], REAL log_t_in, const REAL gout[3], REAL beta_loss, REAL sparsity,
-                        REAL* grad_density, REAL* grad_sh, uint8_t* mask) {
+                        REAL* grad_density, REAL* grad_sh, uint8_t* mask, REAL* accum_out, REAL* log_t_out) {
   const int bd = g->basis_dim, C = 3 * bd;
   const int64_t offy = g->size[2], offx = (int64_t)g->size[1] * g->size[2];
   const int64_t co[8] = {0, 1, offy, offy + 1, offx, offx + 1, offx + offy, offx + offy + 1};
   const REAL log_stop = FN(log_stop)(opt->stop_thresh), step = (REAL)opt->step;
-  REAL basis[9], t, lt = 0, ws, accum;
+  REAL basis[9], t, lt = 0, ws, accum, beta_term = 0;
   FN(ray_t) r;
   int c, j;
   FN(calc_sh)(bd, dir, basis);
   FN(find_bounds)(&r, org, dir, g, opt);
-  if (r.tmin > r.tmax) return;
   accum = FMA(color[0], gout[0], FMA(color[1], gout[1], color[2] * gout[2]));
+  *accum_out = accum;
+  *log_t_out = 0;
+  if (r.tmin > r.tmax) return;
   if (beta_loss > 0) {
     const REAL tin = EXP(log_t_in);
-    beta_loss = (REAL)((double)beta_loss * (1.0 - (double)tin / ((double)((REAL)1 - tin) + 1e-3)));
-    accum += beta_loss;
+    beta_term = (REAL)((double)beta_loss * (1.0 - (double)tin / ((double)((REAL)1 - tin) + 1e-3)));
+    accum += beta_term;
   }
   t = r.tmin;
   ws = r.world_step;
@@ -353,6 +358,213 @@ static void FN(bwd_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const R
     }
     t = t + step;
   }
+  *accum_out = accum - beta_term;
+  *log_t_out = lt;
+}
+
+/* ---- MSI background.
+ * CUDA semantics (opt->bg_cpu == 0): render_background_forward / _backward,
+ * render_lerp_kernel_cuvol.cu:386-607, with ray_find_bounds_bg (render_util.cuh:630-676),
+ * _unitvec2equirect (render_util.cuh:482-490), trilerp_bg_one / trilerp_backward_bg_one
+ * (render_util.cuh:155-232).  Shell i of n = int(nlayers / step) + 2 has radius
+ * n / (n - i - 0.5); the ray is sampled at its far intersection with the shell, and the
+ * sample's optical depth is sigma * world_step * (1/r_prev - 1/r).
+ * Pure-PyTorch semantics (opt->bg_cpu == 1, svox2/svox2.py:796-876): the sample sits at
+ * the midpoint between consecutive far intersections and its optical depth is
+ * sigma * world_step * (t - t_prev); there is no early stop.  This variant exists only to
+ * pin the pieces both share against the reference's own outputs. */
+typedef struct {
+  REAL o[3], d[3], ws, inner;
+  int n_steps;
+} FN(bgray_t);
+
+static void FN(bg_setup)(FN(bgray_t) * b, const REAL org[3], const REAL dir[3], const oracle_grid_t* g,
+                         const oracle_opt_t* opt) {
+  int i;
+  REAL ds, inorm, c[3];
+  for (i = 0; i < 3; ++i) {
+    b->o[i] = FMA(org[i], (REAL)g->scaling[i], (REAL)g->offset[i]);
+    b->d[i] = dir[i] * (REAL)g->scaling[i];
+  }
+  ds = FN(rnorm3)(b->d[0], b->d[1], b->d[2]);
+  for (i = 0; i < 3; ++i) b->d[i] = b->d[i] * ds;
+  for (i = 0; i < 3; ++i) {
+    const REAL sc = (REAL)2 / (REAL)g->size[i];
+    b->o[i] = FMA(b->o[i] + (REAL)0.5, sc, (REAL)-1);
+    b->d[i] = b->d[i] * sc;
+  }
+  inorm = FN(rnorm3)(b->d[0], b->d[1], b->d[2]);
+  b->ws = ds * inorm;
+  for (i = 0; i < 3; ++i) b->d[i] = b->d[i] * inorm;
+  /* _dist_ray_to_origin (cuda_util.cuh:112-119): |o x d| */
+  c[0] = b->o[1] * b->d[2] - b->o[2] * b->d[1];
+  c[1] = b->o[2] * b->d[0] - b->o[0] * b->d[2];
+  c[2] = b->o[0] * b->d[1] - b->o[1] * b->d[0];
+  b->inner = FMAX((REAL)sqrt((double)c[0] * c[0] + (double)c[1] * c[1] + (double)c[2] * c[2]) + (REAL)1e-3f,
+                  (REAL)1);
+  b->n_steps = (int)((float)g->bg_nlayers / opt->step) + 2;
+}
+
+static REAL FN(bg_fetch)(const oracle_grid_t* g, int64_t u, int l2, REAL p2, int ch) {
+  const int32_t lk = g->bg_links[u];
+  const float* p;
+  if (lk < 0) return 0;
+  p = g->bg_data + ((int64_t)lk * g->bg_nlayers + l2) * 4 + ch;
+  return FN(lerp)((REAL)p[0], (REAL)p[4], p2);
+}
+
+/* trilerp_bg_one: layers first, then y (wrapping at reso), then x (wrapping at 2 reso). */
+static REAL FN(bg_trilerp)(const oracle_grid_t* g, const int l[3], const REAL pos[3], int ch) {
+  const int64_t reso = g->bg_reso;
+  const int ny = l[1] < reso - 1 ? l[1] + 1 : 0, nx = l[0] < 2 * reso - 1 ? l[0] + 1 : 0;
+  const REAL ix0 = FN(lerp)(FN(bg_fetch)(g, reso * l[0] + l[1], l[2], pos[2], ch),
+                            FN(bg_fetch)(g, reso * l[0] + ny, l[2], pos[2], ch), pos[1]);
+  const REAL ix1 = FN(lerp)(FN(bg_fetch)(g, reso * nx + l[1], l[2], pos[2], ch),
+                            FN(bg_fetch)(g, reso * nx + ny, l[2], pos[2], ch), pos[1]);
+  return FN(lerp)(ix0, ix1, pos[0]);
+}
+
+static void FN(bg_add)(const oracle_grid_t* g, int64_t u, int l2, REAL p2, const REAL v[4], REAL* grad,
+                       uint8_t* mask) {
+  const int32_t lk = g->bg_links[u];
+  int64_t row;
+  int ch;
+  if (lk < 0) return;
+  row = (int64_t)lk * g->bg_nlayers + l2;
+  for (ch = 0; ch < 4; ++ch) {
+    FN(atomic_add)(grad + row * 4 + ch, v[ch] * ((REAL)1 - p2));
+    FN(atomic_add)(grad + (row + 1) * 4 + ch, v[ch] * p2);
+  }
+  if (mask) mask[row] = mask[row + 1] = 1;
+}
+
+/* trilerp_backward_bg_one for the three colour channels and sigma at once. */
+static void FN(bg_scatter)(const oracle_grid_t* g, const int l[3], const REAL pos[3], const REAL gch[4],
+                           REAL* grad, uint8_t* mask) {
+  const int64_t reso = g->bg_reso;
+  const int ny = l[1] < reso - 1 ? l[1] + 1 : 0, nx = l[0] < 2 * reso - 1 ? l[0] + 1 : 0;
+  const REAL ay = (REAL)1 - pos[1];
+  const int64_t u[4] = {reso * l[0] + l[1], reso * l[0] + ny, reso * nx + l[1], reso * nx + ny};
+  const REAL wy[4] = {ay, pos[1], ay, pos[1]};
+  const REAL wx[4] = {(REAL)1 - pos[0], (REAL)1 - pos[0], pos[0], pos[0]};
+  int k, ch;
+  for (k = 0; k < 4; ++k) {
+    REAL v[4];
+    for (ch = 0; ch < 4; ++ch) v[ch] = wy[k] * (wx[k] * gch[ch]);
+    FN(bg_add)(g, u[k], l[2], pos[2], v, grad, mask);
+  }
+}
+
+/* One ray's background.  gout NULL: forward, adds the background (and the brightness
+ * term) to out.  Otherwise backward: accum is what the foreground left, gradients go to
+ * grad_bg / mask_bg. */
+static void FN(bg_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const REAL org[3], const REAL dir[3],
+                       REAL lt, const REAL* gout, REAL accum, REAL sparsity, REAL out[3], REAL* grad_bg,
+                       uint8_t* mask_bg) {
+  const REAL C0 = (REAL)0.28209479177387814f;
+  const int nl = g->bg_nlayers, cpu = opt->bg_cpu;
+  const REAL log_stop = cpu ? (REAL)(-INFINITY) : FN(log_stop)(opt->stop_thresh);
+  const double inv_pi = 0.31830988618379067154;
+  FN(bgray_t) b;
+  REAL invr_last, t_last = 0, outv[3] = {0, 0, 0};
+  int i, j, c;
+  FN(bg_setup)(&b, org, dir, g, opt);
+  invr_last = (REAL)1 / b.inner;
+  if (cpu) FN(sphere_hit)(b.o, b.d, b.inner, &t_last, 0);
+  for (i = 0; i < b.n_steps; ++i) {
+    const REAL r = (REAL)((double)b.n_steps / ((double)(b.n_steps - i) - 0.5));
+    REAL t, p[3], pos[3], invr, width, sigma;
+    int l[3];
+    if (r < b.inner || !FN(sphere_hit)(b.o, b.d, r, &t, 0)) continue;
+    if (cpu) {
+      const REAL tm = (t + t_last) * (REAL)0.5;
+      for (j = 0; j < 3; ++j) p[j] = b.o[j] + tm * b.d[j];
+    } else {
+      for (j = 0; j < 3; ++j) p[j] = FMA(t, b.d[j], b.o[j]);
+    }
+    invr = FN(rnorm3)(p[0], p[1], p[2]);
+    for (j = 0; j < 3; ++j) p[j] = p[j] * invr;
+    {
+      /* y clamped to [-1, 1]: a last-bit excess would make asin NaN */
+      const REAL lat = ASIN(FMIN(FMAX(p[1], (REAL)-1), (REAL)1)), lon = ATAN2(p[0], p[2]);
+      pos[0] = (REAL)((double)(g->bg_reso * 2) * (0.5 + (double)lon * 0.5 * inv_pi));
+      pos[1] = (REAL)((double)g->bg_reso * (0.5 - (double)lat * inv_pi));
+    }
+    pos[2] = FMIN(FMAX(((REAL)1 - invr) * (REAL)nl - (REAL)0.5, (REAL)0), (REAL)(nl - 1));
+    /* truncation toward zero, as the device's conversion; a NaN or negative coordinate is cell 0 */
+    for (j = 0; j < 3; ++j) l[j] = pos[j] > 0 ? (int)pos[j] : 0;
+    if (l[0] > 2 * g->bg_reso - 1) l[0] = 2 * g->bg_reso - 1;
+    if (l[1] > g->bg_reso - 1) l[1] = g->bg_reso - 1;
+    if (l[2] > nl - 2) l[2] = nl - 2;
+    for (j = 0; j < 3; ++j) pos[j] = pos[j] - (REAL)l[j];
+    sigma = FN(bg_trilerp)(g, l, pos, 3);
+    width = cpu ? t - t_last : invr_last - invr;
+    if (sigma > 0) {
+      const REAL pcnt = cpu ? b.ws * sigma * width : width * b.ws * sigma;
+      const REAL w = EXP(lt) * ((REAL)1 - EXP(-pcnt));
+      lt = lt - pcnt;
+      if (gout == NULL) {
+        for (c = 0; c < 3; ++c) outv[c] = outv[c] + w * FMAX(FN(bg_trilerp)(g, l, pos, c) * C0 + (REAL)0.5, (REAL)0);
+      } else {
+        REAL tc = 0, gch[4];
+        for (c = 0; c < 3; ++c) {
+          const REAL col = FN(bg_trilerp)(g, l, pos, c) * C0 + (REAL)0.5;
+          tc = tc + FMAX(col, (REAL)0) * gout[c];
+          gch[c] = col > 0 ? C0 * w * gout[c] : (REAL)0;
+        }
+        accum = accum - w * tc;
+        gch[3] = b.ws * width * (tc * EXP(lt) - accum);
+        if (sparsity > 0) gch[3] += sparsity * ((REAL)4 * sigma / ((REAL)1 + (REAL)2 * (sigma * sigma)));
+        if (grad_bg) FN(bg_scatter)(g, l, pos, gch, grad_bg, mask_bg);
+      }
+      if (lt < log_stop) break;
+    }
+    invr_last = invr;
+    t_last = t;
+  }
+  if (gout == NULL)
+    for (c = 0; c < 3; ++c) out[c] = out[c] + (outv[c] + EXP(lt) * (REAL)opt->bg);
+}
+
+/* msi_tv_grad_sparse, svox2/csrc/loss_kernel.cu:248-333 (host 606-641): TV of the MSI
+ * over the listed cells (index = (x * reso + y) * nlayers + z), one term per channel,
+ * with forward differences in x and y that wrap and in z that stop at the last layer;
+ * scale (colour channels) and scale_last (the last channel) are divided by the cell count. */
+void FN(oracle_msi_tv_grad)(const int32_t* links, int size0, int size1, const float* msi, int nl, int nc,
+                            const int32_t* cells, int64_t ncells, float scale, float scale_last, REAL* grad,
+                            uint8_t* mask) {
+  const float s_col = scale / (float)ncells, s_last = scale_last / (float)ncells;
+  int64_t q;
+  for (q = 0; q < ncells * nc; ++q) {
+    const int ch = (int)(q % nc), idx = cells[q / nc];
+    const int z = idx % nl, tmp = idx / nl, y = tmp % size1, x = tmp / size1;
+    const int nx = x == size0 - 1 ? 0 : x + 1, ny = y == size1 - 1 ? 0 : y + 1;
+    const int32_t l00 = links[(int64_t)x * size1 + y], l01 = links[(int64_t)x * size1 + ny],
+                  l10 = links[(int64_t)nx * size1 + y];
+    const REAL v00 = l00 >= 0 ? (REAL)msi[((int64_t)l00 * nl + z) * nc + ch] : 0;
+    const REAL vz = (l00 >= 0 && z + 1 < nl) ? (REAL)msi[((int64_t)l00 * nl + z + 1) * nc + ch]
+                                             : (ch == nc - 1 ? (REAL)0 : v00);
+    const REAL v01 = l01 >= 0 ? (REAL)msi[((int64_t)l01 * nl + z) * nc + ch] : 0;
+    const REAL v10 = l10 >= 0 ? (REAL)msi[((int64_t)l10 * nl + z) * nc + ch] : 0;
+    const REAL sc = (REAL)(ch == nc - 1 ? s_last : s_col);
+    REAL dx = v10 - v00, dy = v01 - v00, dz = vz - v00;
+    const REAL idelta = sc * (REAL)(1.0 / sqrt((double)(((REAL)1e-9f + dx * dx) + dy * dy) + (double)(dz * dz)));
+    REAL sm;
+    dx = dx * ((REAL)size0 * ((REAL)1 / (REAL)256));
+    dy = dy * ((REAL)size1 * ((REAL)1 / (REAL)256));
+    dz = dz * ((REAL)nl * ((REAL)1 / (REAL)256));
+    sm = -(dx + dy + dz);
+#define MSI_ADD(link, zz, val)                                              \
+  if ((link) >= 0 && (val) != 0) {                                          \
+    grad[((int64_t)(link) * nl + (zz)) * nc + ch] += (val) * idelta;        \
+    if (mask) mask[(int64_t)(link) * nl + (zz)] = 1;                        \
+  }
+    MSI_ADD(l00, z, sm);
+    if (z + 1 < nl) MSI_ADD(l00, z + 1, dz);
+    MSI_ADD(l01, z, dy);
+    MSI_ADD(l10, z, dx);
+#undef MSI_ADD
+  }
 }
 
 /* Batch over rays: volume_render_cuvol / _fused / _backward
@@ -363,14 +575,15 @@ static void FN(bwd_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const R
 void FN(oracle_render)(const oracle_grid_t* g, const oracle_opt_t* opt, const float* origins, const float* dirs,
                        int64_t Q, int mode, const float* rgb_gt, const float* grad_out, float beta_loss,
                        float sparsity, REAL* rgb_out, REAL* grad_density, REAL* grad_sh, uint8_t* mask,
-                       uint64_t* trace, uint64_t* n_eval_total, int nthreads) {
+                       REAL* grad_bg, uint8_t* mask_bg, uint64_t* trace, uint64_t* n_eval_total, int nthreads) {
   int64_t q;
   uint64_t total = 0;
   const REAL norm = (REAL)2.f / (REAL)(float)(3 * Q);
   if (nthreads < 1) nthreads = 1;
 #pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads) reduction(+ : total)
   for (q = 0; q < Q; ++q) {
-    REAL org[3], dir[3], out[3], gout[3], lt = 0;
+    REAL org[3], dir[3], out[3], gout[3], lt = 0, acc_b = 0, lt_b = 0;
+    const int bg = g->bg_nlayers > 0;
     uint64_t ne = 0;
     int i;
     for (i = 0; i < 3; ++i) {
@@ -379,18 +592,25 @@ void FN(oracle_render)(const oracle_grid_t* g, const oracle_opt_t* opt, const fl
     }
     if (mode == 0 || mode == 1) {
       FN(fwd_ray)(g, opt, org, dir, out, &lt, trace ? trace + q : NULL, &ne);
+      /* render_background_kernel skips rays whose log transmittance is below -25 */
+      if (bg && lt >= (REAL)-25) FN(bg_ray)(g, opt, org, dir, lt, NULL, 0, 0, out, NULL, NULL);
       for (i = 0; i < 3; ++i) rgb_out[q * 3 + i] = out[i];
     }
     if (mode == 1) {
       for (i = 0; i < 3; ++i) gout[i] = (out[i] - (REAL)rgb_gt[q * 3 + i]) * norm;
       FN(bwd_ray)(g, opt, org, dir, out, lt, gout, (REAL)beta_loss / (REAL)Q, (REAL)sparsity, grad_density,
-                  grad_sh, mask);
+                  grad_sh, mask, &acc_b, &lt_b);
+      /* the fused path's background backward starts from the forward's log transmittance */
+      if (bg && lt >= (REAL)-25)
+        FN(bg_ray)(g, opt, org, dir, lt, gout, acc_b, (REAL)sparsity, NULL, grad_bg, mask_bg);
     } else if (mode == 2) {
       for (i = 0; i < 3; ++i) {
         out[i] = rgb_out[q * 3 + i];
         gout[i] = (REAL)grad_out[q * 3 + i];
       }
-      FN(bwd_ray)(g, opt, org, dir, out, 0, gout, 0, 0, grad_density, grad_sh, NULL);
+      FN(bwd_ray)(g, opt, org, dir, out, 0, gout, 0, 0, grad_density, grad_sh, NULL, &acc_b, &lt_b);
+      /* volume_render_cuvol_backward: from the backward pass's own log transmittance */
+      if (bg && lt_b >= (REAL)-25) FN(bg_ray)(g, opt, org, dir, lt_b, gout, acc_b, 0, NULL, grad_bg, NULL);
     }
     total += ne;
   }
@@ -535,6 +755,7 @@ void FN(oracle_render_image)(const oracle_grid_t* g, const oracle_opt_t* opt, co
     int i;
     FN(camera_ray)((int)(q % cam->width), (int)(q / cam->width), cam, dir, org);
     FN(fwd_ray)(g, opt, org, dir, rgb, &lt, trace ? trace + q : NULL, &ne);
+    if (g->bg_nlayers > 0 && lt >= (REAL)-25) FN(bg_ray)(g, opt, org, dir, lt, NULL, 0, 0, rgb, NULL, NULL);
     for (i = 0; i < 3; ++i) out[q * 3 + i] = rgb[i];
   }
 }

@@ -16,11 +16,16 @@ typedef struct {
   int size[3];
   int basis_dim;
   float offset[3], scaling[3];
+  /* MSI background (bg_nlayers == 0: none): links [2*reso, reso], data [capacity, nlayers, 4] */
+  const int32_t* bg_links;
+  const float* bg_data;
+  int bg_reso, bg_nlayers;
 } oracle_grid_t;
 
 typedef struct {
   float bg, step, sigma_thresh, stop_thresh, near_clip;
   int spheric, last_opaque;
+  int bg_cpu; /* background semantics: 0 the CUDA kernels', 1 the pure-PyTorch path's */
 } oracle_opt_t;
 
 typedef struct {
@@ -39,6 +44,8 @@ typedef struct {
 #define FMIN fminf
 #define CEIL ceilf
 #define NEXTAFTER nextafterf
+#define ASIN asinf
+#define ATAN2 atan2f
 #include "oracle_impl.h"
 #undef REAL
 #undef SUFFIX
@@ -49,6 +56,8 @@ typedef struct {
 #undef FMIN
 #undef CEIL
 #undef NEXTAFTER
+#undef ASIN
+#undef ATAN2
 
 #define REAL double
 #define SUFFIX _f64
@@ -59,6 +68,8 @@ typedef struct {
 #define FMIN fmin
 #define CEIL ceil
 #define NEXTAFTER nextafter
+#define ASIN asin
+#define ATAN2 atan2
 #include "oracle_impl.h"
 
 /* accel_dist_prop, svox2/csrc/misc_kernel.cu:108-181 (kernels) and 356-416 (host):

@@ -40,6 +40,10 @@ class SvxGrid(C.Structure):
         ("background_nlayers", C.c_int32),
         ("offset", C.c_float * 3),
         ("scaling", C.c_float * 3),
+        ("background_links", C.c_void_p),
+        ("background_data", C.c_void_p),
+        ("background_capacity", C.c_int64),
+        ("background_reso", C.c_int32),
     ]
 
 
@@ -75,7 +79,8 @@ class SvxRenderOpts(C.Structure):
 
 
 class SvxGridGrads(C.Structure):
-    _fields_ = [("grad_density_out", C.c_void_p), ("grad_sh_out", C.c_void_p), ("mask_out", C.c_void_p)]
+    _fields_ = [("grad_density_out", C.c_void_p), ("grad_sh_out", C.c_void_p), ("mask_out", C.c_void_p),
+                ("grad_background_out", C.c_void_p), ("mask_background_out", C.c_void_p)]
 
 
 class SvxRenderStats(C.Structure):
@@ -121,6 +126,7 @@ SIGNATURES = {
     "svx_tv_grad": [_vp, P(_i32), P(SvxTable), _i32, _i32, _f32, _i32, _f32, _i32, _f32, _f32, _vp, _vp],
     "svx_tv_grad_sparse": [_vp, P(_i32), P(SvxTable), _vp, _i64, _vp, _i32, _i32, _f32, _i32, _f32, _i32,
                            _i32, _f32, _f32, _vp, _vp],
+    "svx_msi_tv_grad_sparse": [_vp, _i32, _vp, _i64, _i32, _i32, _vp, _i64, _vp, _f32, _f32, _vp, _vp],
     "svx_rmsprop_step": [_vp, _i32, _vp, _vp, _i64, _i32, _i32, _vp, _i64, _f32, _f32, _f32, _f32, _f32, _vp],
     "svx_sgd_step": [_vp, _i32, _vp, _i64, _i32, _i32, _vp, _i64, _f32, _f32, _vp],
     "svx_last_error": [],

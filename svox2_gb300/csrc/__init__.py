@@ -9,9 +9,8 @@ on the current PyTorch stream of the data's device and never synchronises
 the host (the reference used the legacy default stream, and ``sample_grid``
 created and synchronised two private streams per call).
 
-Operators this library leaves out (nvol/svox1 backends, MSI background,
-lumisphere TV, dilate, grid_weight_render, the ``tv`` value) are not
-exported, so ``name in csrc.__dict__`` checks like the reference's
+Operators this library leaves out (the nvol/svox1 backends, lumisphere TV)
+are not exported, so ``name in csrc.__dict__`` checks like the reference's
 ``volume_render_image`` dispatch behave as with a module that lacks them.
 """
 from __future__ import annotations
@@ -28,7 +27,7 @@ __all__ = [
     "volume_render_cuvol", "volume_render_cuvol_image", "volume_render_cuvol_backward",
     "volume_render_cuvol_fused", "sample_grid", "sample_grid_backward", "tv_grad",
     "tv_grad_sparse", "rmsprop_step", "sgd_step", "accel_dist_prop", "volume_render_expected_term",
-    "volume_render_sigma_thresh", "dilate", "grid_weight_render", "tv",
+    "volume_render_sigma_thresh", "dilate", "grid_weight_render", "tv", "msi_tv_grad_sparse",
 ]
 
 _DTYPES = {torch.float32: _lib.SVX_F32, torch.bfloat16: _lib.SVX_BF16, torch.float16: _lib.SVX_F16}
@@ -138,8 +137,17 @@ def _grid_struct(grid: SparseGridSpec) -> _lib.SvxGrid:
     _check(sh.dtype in _DTYPES, f"sh_data dtype {sh.dtype} not supported (float32, bfloat16, float16)")
     _check(dens.device == sh.device == links.device, "grid tensors must be on one device")
     _check(sh.size(0) == dens.size(0), "density_data and sh_data row counts differ")
-    if grid.background_links is not None and grid.background_links.numel() > 0:
-        raise RuntimeError("MSI background (background_links) is not supported by svox2_gb300")
+    bl = grid.background_links
+    has_bg = bl is not None and bl.numel() > 0
+    if has_bg:
+        # SparseGridSpec::check, data_spec.hpp:36-41, plus the kernel's 4 channels per layer
+        bl = _cuda_input(bl, "background_links")
+        bd = _cuda_input(grid.background_data, "background_data")
+        _check(bl.ndim == 2 and bl.dtype == torch.int32, "background_links must be int32 [2 * reso, reso]")
+        _check(bl.size(0) == 2 * bl.size(1), "background_links must be [2 * reso, reso]")
+        _check(bd.ndim == 3 and bd.dtype == torch.float32, "background_data must be float32 [N, nlayers, 4]")
+        _check(bd.size(2) == 4 and bd.size(1) >= 2, "background_data must have 4 channels and >= 2 layers")
+        _check(bl.device == bd.device == links.device, "background tables must be on the grid's device")
     _check(off.numel() == 3 and scl.numel() == 3, "_offset and _scaling must have 3 elements")
     offv = off.to(torch.float32).tolist()
     sclv = scl.to(torch.float32).tolist()
@@ -156,6 +164,12 @@ def _grid_struct(grid: SparseGridSpec) -> _lib.SvxGrid:
     g.background_nlayers = 0
     g.offset = (C.c_float * 3)(*offv)
     g.scaling = (C.c_float * 3)(*sclv)
+    if has_bg:
+        g.background_nlayers = bd.size(1)
+        g.background_links = bl.data_ptr()
+        g.background_data = bd.data_ptr()
+        g.background_capacity = bd.size(0)
+        g.background_reso = bl.size(1)
     return g
 
 
@@ -175,8 +189,12 @@ def _opt_struct(opt: RenderOptions) -> _lib.SvxRenderOpts:
                               int(bool(opt.last_sample_opaque)))
 
 
+def _bg_shape(grid: SparseGridSpec, g: _lib.SvxGrid) -> Optional[Tuple[int, ...]]:
+    return tuple(grid.background_data.shape) if g.background_nlayers > 0 else None
+
+
 def _grads_struct(grads: GridOutputGrads, n_vox: int, C_: int, dev: torch.device,
-                  with_mask: bool) -> _lib.SvxGridGrads:
+                  with_mask: bool, bg_shape: Optional[Tuple[int, ...]] = None) -> _lib.SvxGridGrads:
     g = _lib.SvxGridGrads()
     if grads.grad_density_out is not None:
         t = _cuda_input(grads.grad_density_out, "grad_density_out")
@@ -193,6 +211,18 @@ def _grads_struct(grads: GridOutputGrads, n_vox: int, C_: int, dev: torch.device
         _check(t.dtype == torch.bool and t.numel() == n_vox and t.device == dev,
                "mask_out must be bool [N] on the grid's device")
         g.mask_out = t.data_ptr()
+    if bg_shape is not None:
+        if grads.grad_background_out is not None:
+            t = _cuda_input(grads.grad_background_out, "grad_background_out")
+            _check(t.dtype == torch.float32 and tuple(t.shape) == tuple(bg_shape) and t.device == dev,
+                   "grad_background_out must be float32 shaped like background_data on the grid's device")
+            g.grad_background_out = t.data_ptr()
+        mb = grads.mask_background_out
+        if mb is not None and mb.numel() > 0:
+            t = _cuda_input(mb, "mask_background_out")
+            _check(t.dtype == torch.bool and t.numel() == bg_shape[0] * bg_shape[1] and t.device == dev,
+                   "mask_background_out must be bool [N, nlayers] on the grid's device")
+            g.mask_background_out = t.data_ptr()
     return g
 
 
@@ -286,7 +316,7 @@ def volume_render_cuvol_backward(grid: SparseGridSpec, rays: RaysSpec, opt: Rend
     cc = None
     if color_cache is not None:
         cc = _cuda_input(color_cache, "color_cache")
-    gg = _grads_struct(grads, g.n_voxels, g.sh_data_dim, dev, with_mask=False)
+    gg = _grads_struct(grads, g.n_voxels, g.sh_data_dim, dev, with_mask=False, bg_shape=_bg_shape(grid, g))
     with torch.cuda.device(dev):
         _lib.call("svx_volume_render_cuvol_backward", C.byref(g), C.byref(r), C.byref(_opt_struct(opt)),
                   go.data_ptr(), _ptr(cc), C.byref(gg), _stats_struct(stats), _stream(dev))
@@ -303,7 +333,7 @@ def volume_render_cuvol_fused(grid: SparseGridSpec, rays: RaysSpec, opt: RenderO
     out = _cuda_input(rgb_out, "rgb_out")
     _check(gt.dtype == torch.float32 and gt.shape == rays.origins.shape, "rgb_gt must be float32 [Q, 3]")
     _check(out.dtype == torch.float32 and out.shape == rays.origins.shape, "rgb_out must be float32 [Q, 3]")
-    gg = _grads_struct(grads, g.n_voxels, g.sh_data_dim, dev, with_mask=True)
+    gg = _grads_struct(grads, g.n_voxels, g.sh_data_dim, dev, with_mask=True, bg_shape=_bg_shape(grid, g))
     with torch.cuda.device(dev):
         _lib.call("svx_volume_render_cuvol_fused", C.byref(g), C.byref(r), C.byref(_opt_struct(opt)),
                   gt.data_ptr(), float(beta_loss), float(sparsity_loss), out.data_ptr(), C.byref(gg),
@@ -455,6 +485,30 @@ def tv_grad_sparse(links: torch.Tensor, data: torch.Tensor, rand_cells: torch.Te
                   mk.data_ptr() if use_mask else None, int(start_dim), int(end_dim), float(scale),
                   int(bool(use_logalpha)), float(logalpha_delta), int(bool(ignore_edge)),
                   int(bool(ignore_last_z)), float(ndc_coeffx), float(ndc_coeffy), gd.data_ptr(), _stream(dev))
+
+
+def msi_tv_grad_sparse(links: torch.Tensor, msi: torch.Tensor, rand_cells: torch.Tensor, mask_out: torch.Tensor,
+                       scale: float, scale_last: float, grad_msi: torch.Tensor) -> None:
+    """svox2/csrc/loss_kernel.cu:606-641: TV gradient of the MSI background on a list of cells."""
+    lk = _cuda_input(links, "links")
+    m = _cuda_input(msi, "msi")
+    rc = _cuda_input(rand_cells, "rand_cells")
+    mk = _cuda_input(mask_out, "mask_out")
+    gd = _cuda_input(grad_msi, "grad_msi")
+    _check(lk.dtype == torch.int32 and lk.ndim == 2 and lk.size(0) == 2 * lk.size(1),
+           "links must be int32 [2 * reso, reso]")
+    _check(m.dtype == torch.float32 and m.ndim == 3, "msi must be float32 [N, nlayers, channels]")
+    _check(gd.dtype == torch.float32 and gd.shape == m.shape, "grad_msi must be float32 shaped like msi")
+    _check(rc.dtype == torch.int32 and rc.ndim == 1, "rand_cells must be int32 [n]")
+    use_mask = mk.dim() > 0 and mk.size(0) > 0
+    if use_mask:
+        _check(mk.dtype == torch.bool and mk.numel() == m.size(0) * m.size(1), "mask_out must be bool [N, nlayers]")
+    _check(lk.device == m.device == rc.device == gd.device, "tensors must be on one device")
+    dev = m.device
+    with torch.cuda.device(dev):
+        _lib.call("svx_msi_tv_grad_sparse", lk.data_ptr(), lk.size(1), m.data_ptr(), m.size(0), m.size(1), m.size(2),
+                  rc.data_ptr(), rc.size(0), mk.data_ptr() if use_mask else None, float(scale), float(scale_last),
+                  gd.data_ptr(), _stream(dev))
 
 
 # ---------------------------------------------------------------- optimisers

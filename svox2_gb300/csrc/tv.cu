@@ -1,8 +1,9 @@
 // Total variation on the voxel grid: its value and its gradients.
 //
 // Replaces svox2/csrc/loss_kernel.cu: tv_kernel 42-109 (the value), tv_grad_kernel 111-176 (dense over all
-// cells) and tv_grad_sparse_kernel 178-246 (a list of cells, the training
-// default), with their host launchers 522-604.  One thread per (cell, channel),
+// cells), tv_grad_sparse_kernel 178-246 (a list of cells, the training
+// default) and msi_tv_grad_sparse_kernel 248-333 (the MSI background), with
+// their host launchers 483-641.  One thread per (cell, channel),
 // channels innermost so that a warp reads consecutive coefficients of the same
 // voxel rows.  The reference's edge conventions are kept exactly:
 //   * sparse: a neighbour outside the grid reads link 0 (voxel 0), not -1;
@@ -193,6 +194,64 @@ unsigned grid_for(long long total) {
   return (unsigned)(b < 1 ? 1 : b);
 }
 
+// msi_tv_grad_sparse_kernel, loss_kernel.cu:248-333: TV of the MSI background, one thread per
+// (listed cell, channel), channels innermost.  x (2 reso columns) and y (reso rows) wrap; z
+// stops at the last layer, where the colour channels compare with themselves and sigma with 0.
+struct MsiArgs {
+  const int32_t* links;
+  int X, Y;  // 2 reso, reso
+  const float* msi;
+  long long capacity;  // rows of msi
+  int nl, nc;
+  float scale, scale_last;  // already divided by the number of cells
+  float* grad;
+  uint8_t* mask;
+};
+
+__global__ void __launch_bounds__(256) msi_tv_kernel(MsiArgs a, const int32_t* __restrict__ cells, long long n) {
+  const long long total = n * a.nc;
+  const long long n_cells_all = (long long)a.X * a.Y * a.nl;
+  const float sx = a.X * (1.f / 256.f), sy = a.Y * (1.f / 256.f), sz = a.nl * (1.f / 256.f);
+  for (long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x; tid < total;
+       tid += (long long)gridDim.x * blockDim.x) {
+    const int ch = (int)(tid % a.nc);
+    const int idx = __ldg(cells + tid / a.nc);
+    if (idx < 0 || idx >= n_cells_all) continue;  // cell index outside the MSI
+    const int z = idx % a.nl, xy = idx / a.nl;
+    const int y = xy % a.Y, x = xy / a.Y;
+    const int nx = x == a.X - 1 ? 0 : x + 1, ny = y == a.Y - 1 ? 0 : y + 1;
+    // a link past the data's rows reads as empty, like a negative one
+    auto link = [&](int xx, int yy) {
+      const int l = __ldg(a.links + (long long)xx * a.Y + yy);
+      return l < a.capacity ? l : -1;
+    };
+    const int l00 = link(x, y), l01 = link(x, ny), l10 = link(nx, y);
+    const bool last = ch == a.nc - 1;
+    auto at = [&](int lnk, int zz) { return __ldg(a.msi + ((long long)lnk * a.nl + zz) * a.nc + ch); };
+    const float v00 = l00 >= 0 ? at(l00, z) : 0.f;
+    const float vz = (l00 >= 0 && z + 1 < a.nl) ? at(l00, z + 1) : (last ? 0.f : v00);
+    const float v01 = l01 >= 0 ? at(l01, z) : 0.f;
+    const float v10 = l10 >= 0 ? at(l10, z) : 0.f;
+    float dx = __fsub_rn(v10, v00), dy = __fsub_rn(v01, v00), dz = __fsub_rn(vz, v00);
+    const float idelta =
+        __fmul_rn(last ? a.scale_last : a.scale, rsqrtf(fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, 1e-9f)))));
+    dx = __fmul_rn(dx, sx);
+    dy = __fmul_rn(dy, sy);
+    dz = __fmul_rn(dz, sz);
+    const float sm = -__fadd_rn(__fadd_rn(dx, dy), dz);
+    auto add = [&](int lnk, int zz, float v) {
+      if (lnk >= 0 && v != 0.f) {
+        atomicAdd(a.grad + ((long long)lnk * a.nl + zz) * a.nc + ch, __fmul_rn(v, idelta));
+        if (a.mask != nullptr) a.mask[(long long)lnk * a.nl + zz] = 1;
+      }
+    };
+    add(l00, z, sm);
+    if (z + 1 < a.nl) add(l00, z + 1, dz);
+    add(l01, z, dy);
+    add(l10, z, dx);
+  }
+}
+
 }  // namespace
 }  // namespace svx
 
@@ -282,5 +341,38 @@ extern "C" int svx_tv(const int32_t* links, const int32_t size[3], const svx_tab
     default: tv_value_kernel<__half><<<blocks, 256, 0, st>>>(a, out);
   }
   SVX_LAUNCH_CHECK("tv_value_kernel");
+  return SVX_OK;
+}
+
+extern "C" int svx_msi_tv_grad_sparse(const int32_t* links, int32_t reso, const float* msi, int64_t capacity,
+                                      int32_t nlayers, int32_t n_channels, const int32_t* rand_cells,
+                                      int64_t n_cells, uint8_t* mask_out, float scale, float scale_last,
+                                      float* grad, void* stream) {
+  clear_error();
+  SVX_REQUIRE(links && msi && grad, SVX_ERR_INVALID, "null argument");
+  SVX_REQUIRE(reso >= 1, SVX_ERR_INVALID, "reso = %d must be >= 1", reso);
+  SVX_REQUIRE(nlayers >= 1 && n_channels >= 1, SVX_ERR_INVALID, "nlayers = %d, n_channels = %d must be >= 1",
+              nlayers, n_channels);
+  SVX_REQUIRE(capacity >= 0, SVX_ERR_INVALID, "capacity < 0");
+  SVX_REQUIRE((long long)2 * reso * reso * nlayers < (1ll << 31), SVX_ERR_TOO_LARGE,
+              "the MSI's cell count must fit int32 cell indices");
+  SVX_REQUIRE(n_cells >= 0, SVX_ERR_INVALID, "n_cells < 0");
+  if (n_cells == 0) return SVX_OK;
+  SVX_REQUIRE(rand_cells != nullptr, SVX_ERR_INVALID, "rand_cells is null");
+  MsiArgs a;
+  a.links = links;
+  a.X = 2 * reso;
+  a.Y = reso;
+  a.msi = msi;
+  a.capacity = capacity;
+  a.nl = nlayers;
+  a.nc = n_channels;
+  a.scale = scale / (float)(int)n_cells;
+  a.scale_last = scale_last / (float)(int)n_cells;
+  a.grad = grad;
+  a.mask = mask_out;
+  cudaStream_t st = as_stream(stream);
+  msi_tv_kernel<<<grid_for(n_cells * n_channels), 256, 0, st>>>(a, rand_cells, n_cells);
+  SVX_LAUNCH_CHECK("msi_tv_kernel");
   return SVX_OK;
 }

@@ -9,8 +9,8 @@ CUDA library; there is no CPU path — ``use_kernel=False`` and CPU grids raise.
 
 Additions: ``sh_dtype`` (store SH coefficients as bfloat16 or float16; all
 arithmetic stays float32, gradients and optimiser state are float32).
-Left out (raise NotImplementedError): MSI background, learned/MLP bases,
-nvol/svox1 backends, resampling and the grid-editing utilities.
+Left out (raise NotImplementedError): learned/MLP bases and their optimiser,
+nvol/svox1 backends, resize, svox1 export and lumisphere TV.
 """
 from __future__ import annotations
 
@@ -223,7 +223,8 @@ class _TotalVariationFunction(autograd.Function):
 
 class _VolumeRenderFunction(autograd.Function):
     """svox2/svox2.py:226-288.  The backward is the reverse-order adjoint kernel;
-    the colour it is handed is not needed by it and is kept for interface parity."""
+    the colour it is handed is not needed by it and is kept for interface parity.
+    With the MSI background, its table (data_background) gets a gradient too."""
 
     @staticmethod
     def forward(ctx, data_density, data_sh, data_basis, data_background, grid, rays, opt, backend):
@@ -244,13 +245,17 @@ class _VolumeRenderFunction(autograd.Function):
         holder = _C.GridOutputGrads()
         holder.grad_density_out = grad_density_grid
         holder.grad_sh_out = grad_sh_grid
+        grad_background = None
+        if ctx.grid.background_data is not None and ctx.needs_input_grad[3]:
+            grad_background = torch.zeros_like(ctx.grid.background_data, dtype=torch.float32)
+            holder.grad_background_out = grad_background
         _C.volume_render_cuvol_backward(ctx.grid, ctx.rays, ctx.opt, grad_out.contiguous(), color_cache, holder)
         ctx.grid = ctx.rays = ctx.opt = None
         if not ctx.needs_input_grad[0]:
             grad_density_grid = None
         if not ctx.needs_input_grad[1]:
             grad_sh_grid = None
-        return grad_density_grid, grad_sh_grid, None, None, None, None, None, None
+        return grad_density_grid, grad_sh_grid, None, grad_background, None, None, None, None
 
 
 # ---------------------------------------------------------------- grid
@@ -265,7 +270,8 @@ class SparseGrid(nn.Module):
     :param basis_dim: 1, 4 or 9 (SH degree 0, 1, 2)
     :param use_z_order: Morton order of the initial links (cubic power-of-2 grids)
     :param use_sphere_bound: allocate only voxels within the unit ball
-    :param background_nlayers: must be 0 (svox2_gb300 has no MSI background)
+    :param background_nlayers: 0, or the layer count (>= 2) of the MSI background model
+    :param background_reso: MSI background resolution (equirectangular 2 reso x reso cells per layer)
     :param device: torch device
     :param sh_dtype: storage type of sh_data: torch.float32 (default), bfloat16 or float16
     """
@@ -292,15 +298,14 @@ class SparseGrid(nn.Module):
             raise NotImplementedError("only the SH basis (BASIS_TYPE_SH) is built")
         if basis_dim not in (1, 4, 9):
             raise NotImplementedError("basis_dim must be 1, 4 or 9 (SH degree <= 2)")
-        if background_nlayers != 0:
-            raise NotImplementedError("the MSI background model is not built (background_nlayers must be 0)")
+        assert background_nlayers == 0 or background_nlayers > 1, "Please use at least 2 MSI layers (trilerp limitation)"
         if sh_dtype not in (torch.float32, torch.bfloat16, torch.float16):
             raise ValueError("sh_dtype must be float32, bfloat16 or float16")
         self.basis_type = basis_type
         self.basis_dim = basis_dim
         self.mlp_posenc_size = mlp_posenc_size
         self.mlp_width = mlp_width
-        self.background_nlayers = 0
+        self.background_nlayers = background_nlayers
         self.background_reso = background_reso
 
         if isinstance(reso, int):
@@ -350,9 +355,17 @@ class SparseGrid(nn.Module):
         self.sh_data = nn.Parameter(torch.zeros(self.capacity, self.basis_dim * 3, dtype=sh_dtype, device=device))
         self.basis_data = nn.Parameter(torch.empty(0, 0, 0, 0, dtype=torch.float32, device=device),
                                        requires_grad=False)
-        self.background_data = nn.Parameter(torch.empty(0, 0, 0, dtype=torch.float32, device=device),
-                                            requires_grad=False)
-        self.background_links: Optional[torch.Tensor] = None
+        if self.use_background:
+            # MSI background (svox2/svox2.py:497-512): every cell of every layer allocated
+            bg_cap = 2 * self.background_reso ** 2
+            self.register_buffer("background_links", torch.arange(bg_cap, dtype=torch.int32, device=device)
+                                 .reshape(2 * self.background_reso, self.background_reso))
+            self.background_data = nn.Parameter(torch.zeros(bg_cap, self.background_nlayers, 4,
+                                                            dtype=torch.float32, device=device))
+        else:
+            self.background_data = nn.Parameter(torch.empty(0, 0, 0, dtype=torch.float32, device=device),
+                                                requires_grad=False)
+            self.background_links: Optional[torch.Tensor] = None
         self.register_buffer("links", init_links.view(reso))
         self.links: torch.Tensor
         self.opt = RenderOptions()
@@ -393,7 +406,7 @@ class SparseGrid(nn.Module):
 
     @property
     def use_background(self):
-        return False
+        return self.background_nlayers > 0
 
     @property
     def shape(self):
@@ -425,8 +438,9 @@ class SparseGrid(nn.Module):
         if not use_kernel or not self.links.is_cuda:
             _no_cpu_path("SparseGrid.volume_render")
         assert rays.is_cuda
-        return _VolumeRenderFunction.apply(self.density_data, self.sh_data, None, None, self._to_cpp(),
-                                           rays._to_cpp(), self.opt._to_cpp(randomize=randomize),
+        return _VolumeRenderFunction.apply(self.density_data, self.sh_data, None,
+                                           self.background_data if self.use_background else None,
+                                           self._to_cpp(), rays._to_cpp(), self.opt._to_cpp(randomize=randomize),
                                            self.opt.backend)
 
     def volume_render_fused(self, rays: Rays, rgb_gt: torch.Tensor, randomize: bool = False,
@@ -434,7 +448,8 @@ class SparseGrid(nn.Module):
         """Render and accumulate the MSE gradient into .grad (svox2/svox2.py:1072-1142).
 
         Sets ``sparse_grad_indexer`` (bool [N]: voxels that received a gradient)
-        and ``sparse_sh_grad_indexer`` (a copy), as the reference does.
+        and ``sparse_sh_grad_indexer`` (a copy), as the reference does; with the MSI
+        background also its gradient and ``sparse_background_indexer`` (bool [N_bg, nlayers]).
         """
         if not self.sh_data.is_cuda:
             _no_cpu_path("SparseGrid.volume_render_fused")
@@ -447,6 +462,11 @@ class SparseGrid(nn.Module):
         holder.grad_density_out = grad_density
         holder.grad_sh_out = grad_sh
         holder.mask_out = self.sparse_grad_indexer
+        if self.use_background:
+            holder.grad_background_out = self._grad_buffer(self.background_data)
+            self.sparse_background_indexer = torch.zeros(list(self.background_data.shape[:-1]), dtype=torch.bool,
+                                                         device=self.background_data.device)
+            holder.mask_background_out = self.sparse_background_indexer
         _C.volume_render_cuvol_fused(self._to_cpp(), rays._to_cpp(), self.opt._to_cpp(randomize=randomize),
                                      rgb_gt, beta_loss, sparsity_loss, rgb_out, holder)
         self.sparse_sh_grad_indexer = self.sparse_grad_indexer.clone()
@@ -565,6 +585,22 @@ class SparseGrid(nn.Module):
                        ndc_coeffs[0], ndc_coeffs[1], grad)
             self.sparse_sh_grad_indexer = None
 
+    def inplace_tv_background_grad(self, grad: torch.Tensor, scaling: float = 1.0,
+                                   scaling_density: Optional[float] = None, sparse_frac: float = 0.01,
+                                   contiguous: bool = False):
+        """Add the MSI background's TV gradient into grad (None: background_data's own gradient):
+        colour channels times scaling, sigma times scaling_density (default scaling), over a
+        random set of cells (svox2/svox2.py:1930-1955)."""
+        if grad is None:
+            grad = self._grad_buffer(self.background_data)
+        assert self.background_data.is_cuda and grad.is_cuda, "the grid and grad must be on a CUDA device"
+        rand_cells_bg = self._get_rand_cells_background(sparse_frac, contiguous)
+        indexer = self._get_sparse_background_grad_indexer()
+        if scaling_density is None:
+            scaling_density = scaling
+        _C.msi_tv_grad_sparse(self.background_links, self.background_data, rand_cells_bg, indexer, scaling,
+                              scaling_density, grad)
+
     # ---- optimisers (svox2/svox2.py:1972-2041)
     def optim_density_step(self, lr: float, beta: float = 0.9, epsilon: float = 1e-8, optim: str = "rmsprop"):
         """RMSprop or SGD step on density_data over the voxels the last render touched."""
@@ -594,6 +630,26 @@ class SparseGrid(nn.Module):
         else:
             raise NotImplementedError(f"Unsupported optimizer {optim}")
 
+    def optim_background_step(self, lr_sigma: float, lr_color: float, beta: float = 0.9, epsilon: float = 1e-8,
+                              optim: str = "rmsprop"):
+        """RMSprop or SGD step on the MSI background (svox2/svox2.py:2043-2084): rows are
+        (cell, layer) pairs of four channels, the last (sigma) at lr_sigma, the colours at
+        lr_color, over the rows the last fused render touched."""
+        assert self.background_data.is_cuda, "the grid must be on a CUDA device"
+        indexer = self._maybe_convert_sparse_grad_indexer(bg=True)
+        n_chnl = self.background_data.size(-1)
+        grad = self._grad_buffer(self.background_data)
+        if optim == "rmsprop":
+            if self.background_rms is None or self.background_rms.shape != self.background_data.shape:
+                self.background_rms = torch.zeros_like(self.background_data.data)
+            _C.rmsprop_step(self.background_data.data.view(-1, n_chnl), self.background_rms.view(-1, n_chnl),
+                            grad.view(-1, n_chnl), indexer, beta, lr_color, epsilon, -1e9, lr_sigma)
+        elif optim == "sgd":
+            _C.sgd_step(self.background_data.data.view(-1, n_chnl), grad.view(-1, n_chnl), indexer, lr_color,
+                        lr_sigma)
+        else:
+            raise NotImplementedError(f"Unsupported optimizer {optim}")
+
     # ---- internals (svox2/svox2.py:2135-2241)
     def _to_cpp(self, grid_coords: bool = False, replace_basis_data: Optional[torch.Tensor] = None):
         gspec = _C.SparseGridSpec()
@@ -609,6 +665,9 @@ class SparseGrid(nn.Module):
             gspec._scaling = self._scaling * gsz
         gspec.basis_dim = self.basis_dim
         gspec.basis_type = self.basis_type
+        if self.use_background:
+            gspec.background_links = self.background_links
+            gspec.background_data = self.background_data
         return gspec
 
     def _grid_size(self):
@@ -652,9 +711,35 @@ class SparseGrid(nn.Module):
         mask kernel produces identical results, so the mask is passed as is.
         """
         indexer = self.sparse_sh_grad_indexer if sh else self.sparse_grad_indexer
+        if bg:
+            indexer = self.sparse_background_indexer
+            if indexer is not None:
+                indexer = indexer.view(-1)
         if indexer is None:
             return torch.empty((), device=self.density_data.device)
         return indexer
+
+    def _get_sparse_background_grad_indexer(self):
+        indexer = self.sparse_background_indexer
+        if indexer is None:
+            indexer = torch.empty((0, 0), dtype=torch.bool, device=self.density_data.device)
+        return indexer
+
+    def _get_rand_cells_background(self, sparse_frac: float, contiguous: bool = True):
+        """Random MSI background TV cells over the [2 reso, reso, nlayers] cells, drawn as
+        _get_rand_cells draws them (svox2/svox2.py:2243-2260)."""
+        assert self.use_background, "Can only use sparse background loss if using background"
+        assert self.sparse_background_indexer is None or self.sparse_background_indexer.dtype == torch.bool, \
+            "please call sparse loss after rendering and before gradient updates"
+        grid_size = self.background_links.size(0) * self.background_links.size(1) * self.background_data.size(1)
+        sparse_num = max(int(sparse_frac * grid_size), 1)
+        if contiguous:
+            start = np.random.randint(0, grid_size)
+            arr = torch.arange(start, start + sparse_num, dtype=torch.int32, device=self.links.device)
+            if start > grid_size - sparse_num:
+                arr[grid_size - sparse_num - start:] -= grid_size
+            return arr
+        return torch.randint(0, grid_size, (sparse_num,), dtype=torch.int32, device=self.links.device)
 
     def _get_rand_cells(self, sparse_frac: float, force: bool = False, contiguous: bool = True):
         """Random TV cells: a contiguous (wrapping) window of max(int(frac * n), 1) cells from a
@@ -788,8 +873,11 @@ class SparseGrid(nn.Module):
             "density_data": self.density_data.data.cpu().numpy(),
             # through float32 (exact for bfloat16 / float16) to the file's float16
             "sh_data": self.sh_data.data.float().cpu().numpy().astype(np.float16),
-            "basis_type": self.basis_type,
         }
+        if self.use_background:
+            data["background_links"] = self.background_links.cpu().numpy()
+            data["background_data"] = self.background_data.data.cpu().numpy()
+        data["basis_type"] = self.basis_type
         save_fn(path, **data)
 
     @classmethod
@@ -806,8 +894,6 @@ class SparseGrid(nn.Module):
         else:
             sh_data = z.f.sh_data
             density_data = z.f.density_data
-        if "background_data" in z:
-            raise NotImplementedError("checkpoints with the MSI background model are not supported by svox2_gb300")
         basis_type = z["basis_type"].item() if "basis_type" in z else BASIS_TYPE_SH
         if basis_type != BASIS_TYPE_SH or "basis_data" in z.keys():
             raise NotImplementedError("only SH-basis checkpoints are supported by svox2_gb300")
@@ -818,9 +904,39 @@ class SparseGrid(nn.Module):
         links = torch.from_numpy(np.ascontiguousarray(z.f.links).astype(np.int32))
         grid = cls.from_tables(links.to(device=device), dens.to(device=device),
                                sh.to(device=device, dtype=sh_dtype), radius=radius, center=center)
+        if "background_data" in z:
+            bd = torch.from_numpy(np.ascontiguousarray(z["background_data"])).to(device=device)
+            bl = torch.from_numpy(np.ascontiguousarray(z["background_links"])).to(device=device)
+            grid.background_nlayers = bd.shape[1]
+            grid.background_reso = bl.shape[1]
+            grid.background_data = nn.Parameter(bd)
+            grid.background_links = bl
         if grid.links.is_cuda:
             grid.accelerate()
         return grid
+
+    def sparsify_background(self, sigma_thresh: float = 1.0, dilate: int = 1):
+        """Drop the MSI background cells whose sigma stays below sigma_thresh in every layer,
+        after `dilate` 3x3x3 dilations of the kept (cell, layer) mask, and re-index the rest in
+        raster order (svox2/svox2.py:1426-1448)."""
+        assert self.use_background, "the grid has no MSI background"
+        if int(dilate) > 0 and not self.background_links.is_cuda:
+            raise RuntimeError("sparsify_background dilates with a CUDA kernel: the grid must be on a CUDA device")
+        device = self.background_links.device
+        nl = self.background_nlayers
+        sigma_mask = torch.zeros(list(self.background_links.shape) + [nl], dtype=torch.bool,
+                                 device=device).view(-1, nl)
+        nonempty_mask = self.background_links.view(-1) >= 0
+        data_mask = self.background_data[..., -1] >= sigma_thresh
+        sigma_mask[nonempty_mask] = data_mask   # the rows in raster order of the non-empty cells
+        sigma_mask = sigma_mask.view(list(self.background_links.shape) + [nl])
+        for _ in range(int(dilate)):
+            sigma_mask = _C.dilate(sigma_mask)
+        sigma_mask = sigma_mask.any(-1) & nonempty_mask.view(self.background_links.shape)
+        self.background_links[~sigma_mask] = -1
+        retain_vals = self.background_links[sigma_mask]
+        self.background_links[sigma_mask] = torch.arange(retain_vals.size(0), dtype=torch.int32, device=device)
+        self.background_data = nn.Parameter(self.background_data.data[retain_vals.long()])
 
     # ---- empty-space skipping
     def accelerate(self):
@@ -835,6 +951,6 @@ class SparseGrid(nn.Module):
     def _unbuilt(self, *a, **k):
         raise NotImplementedError("this SparseGrid method is not implemented in svox2_gb300")
 
-    sparsify_background = resize = to_svox1 = _unbuilt
-    inplace_tv_lumisphere_grad = inplace_tv_background_grad = inplace_tv_basis_grad = _unbuilt
-    optim_background_step = optim_basis_step = _unbuilt
+    resize = to_svox1 = _unbuilt
+    inplace_tv_lumisphere_grad = inplace_tv_basis_grad = _unbuilt
+    optim_basis_step = _unbuilt

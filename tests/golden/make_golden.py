@@ -11,6 +11,9 @@ records inputs and outputs of
   * SparseGrid.save / SparseGrid.load of a checkpoint (svox2/svox2.py:1526-1628),
   * SparseGrid.resample on the CPU path without dilation (svox2/svox2.py:1223-1424),
   * SparseGrid.inplace_l2_color_grad (svox2/svox2.py:1897-1932),
+  * SparseGrid.volume_render(use_kernel=False) with the MSI background model
+    (svox2/svox2.py:796-876) + autograd, save / load of a grid with the background,
+    and SparseGrid.sparsify_background without dilation (svox2/svox2.py:1426-1448),
 into tests/golden/*.npz.  sigma_thresh = stop_thresh = 0 so that the CPU
 path's semantics coincide with the CUDA kernel's (the reference's own
 test/test_render_gradcheck.py uses the same setting).
@@ -77,6 +80,49 @@ def render_case(svox2, name, reso, basis_dim, occupancy, z_order, n_rays, bg, st
     print(name, "rays", n_rays, "voxels", N, "rgb mean", float(rgb.mean()))
 
 
+def background_case(svox2, name, reso, basis_dim, nlayers, bg_reso, n_rays, bg, step, seed):
+    """volume_render(use_kernel=False) of a grid with the MSI background model (svox2/svox2.py:796-876)
+    and the autograd gradients of the MSE loss, background included."""
+    gen = torch.Generator().manual_seed(seed)
+    grid = svox2.SparseGrid(reso=reso, basis_dim=basis_dim, background_nlayers=nlayers, background_reso=bg_reso,
+                            device="cpu")
+    N = grid.density_data.shape[0]
+    dens = torch.clamp(torch.randn((N, 1), generator=gen) * 0.6 + 0.2, min=0.0)
+    sh = torch.randn((N, 3 * basis_dim), generator=gen) * 0.3
+    grid.density_data.data[:] = dens
+    grid.sh_data.data[:] = sh
+    # drop a fifth of the background cells and re-index the rest
+    keep = torch.rand(grid.background_links.shape, generator=gen) >= 0.2
+    bl = torch.full(grid.background_links.shape, -1, dtype=torch.int32)
+    bl[keep] = torch.arange(int(keep.sum()), dtype=torch.int32)
+    grid.background_links = bl
+    bd = torch.randn((int(keep.sum()), nlayers, 4), generator=gen) * 0.5
+    bd[..., 3] = torch.rand((int(keep.sum()), nlayers), generator=gen) * 4.0 - 0.5
+    grid.background_data = torch.nn.Parameter(bd.clone())
+    grid.opt.sigma_thresh = 0.0
+    grid.opt.stop_thresh = 0.0
+    grid.opt.background_brightness = bg
+    grid.opt.step_size = step
+    o, d, gt = _rays(n_rays, gen)
+    # half of the rays leave in random directions: some miss the grid and see only the background
+    h = n_rays // 2
+    dr = torch.randn((n_rays - h, 3), generator=gen)
+    d[h:] = dr / dr.norm(dim=-1, keepdim=True)
+    rgb = grid.volume_render(svox2.Rays(o, d), use_kernel=False)
+    loss = F.mse_loss(rgb, gt)
+    loss.backward()
+    gsz = grid._grid_size()
+    np.savez_compressed(
+        OUT / f"background_{name}.npz",
+        links=grid.links.numpy().astype(np.int32), density=dens.numpy(), sh=sh.numpy(),
+        basis_dim=basis_dim, offset=(grid._offset * gsz - 0.5).numpy(), scaling=(grid._scaling * gsz).numpy(),
+        bg_links=bl.numpy(), bg_data=bd.numpy(),
+        origins=o.numpy(), dirs=d.numpy(), rgb_gt=gt.numpy(), bg=bg, step=step,
+        rgb=rgb.detach().numpy(), grad_density=grid.density_data.grad.numpy(),
+        grad_sh=grid.sh_data.grad.numpy(), grad_background=grid.background_data.grad.numpy())
+    print(name, "rays", n_rays, "bg cells", int(keep.sum()), "rgb mean", float(rgb.mean()))
+
+
 def sample_case(svox2, name, reso, basis_dim, n_points, seed):
     gen = torch.Generator().manual_seed(seed)
     grid = svox2.SparseGrid(reso=reso, basis_dim=basis_dim, device="cpu")
@@ -99,11 +145,13 @@ def sample_case(svox2, name, reso, basis_dim, n_points, seed):
     print(name, "points", n_points)
 
 
-def checkpoint_case(svox2, name, reso, basis_dim, occupancy, radius, center, seed):
+def checkpoint_case(svox2, name, reso, basis_dim, occupancy, radius, center, seed, bg=None):
     """SparseGrid.save (svox2/svox2.py:1526-1553) of a seeded grid, written by the reference
-    itself, plus what the reference's SparseGrid.load (1555-1628) reads back from it."""
+    itself, plus what the reference's SparseGrid.load (1555-1628) reads back from it.
+    bg = (nlayers, reso): the grid also carries an MSI background with a fifth of its cells dropped."""
     gen = torch.Generator().manual_seed(seed)
-    grid = svox2.SparseGrid(reso=reso, basis_dim=basis_dim, radius=radius, center=center, device="cpu")
+    kw = {} if bg is None else {"background_nlayers": bg[0], "background_reso": bg[1]}
+    grid = svox2.SparseGrid(reso=reso, basis_dim=basis_dim, radius=radius, center=center, device="cpu", **kw)
     keep = torch.rand(grid.links.shape, generator=gen) < occupancy
     links = torch.full(grid.links.shape, -1, dtype=torch.int32)
     links[keep] = torch.arange(int(keep.sum()), dtype=torch.int32)
@@ -111,14 +159,46 @@ def checkpoint_case(svox2, name, reso, basis_dim, occupancy, radius, center, see
     grid.links = links
     grid.density_data = torch.nn.Parameter(torch.randn((N, 1), generator=gen) * 3.0)
     grid.sh_data = torch.nn.Parameter(torch.randn((N, 3 * basis_dim), generator=gen) * 0.3)
+    extra = {}
+    if bg is not None:
+        bkeep = torch.rand(grid.background_links.shape, generator=gen) >= 0.2
+        bl = torch.full(grid.background_links.shape, -1, dtype=torch.int32)
+        bl[bkeep] = torch.arange(int(bkeep.sum()), dtype=torch.int32)
+        grid.background_links = bl
+        grid.background_data = torch.nn.Parameter(torch.randn((int(bkeep.sum()), bg[0], 4), generator=gen))
     path = OUT / f"ckpt_{name}.npz"
     grid.save(str(path), compress=True)
     back = svox2.SparseGrid.load(str(path), device="cpu")
+    if bg is not None:
+        extra = dict(background_links=back.background_links.numpy(),
+                     background_data=back.background_data.data.numpy(),
+                     background_nlayers=back.background_nlayers, background_reso=back.background_reso,
+                     src_background_data=grid.background_data.data.numpy())
     np.savez_compressed(
         OUT / f"ckpt_{name}_loaded.npz", links=back.links.numpy(), density_data=back.density_data.data.numpy(),
         sh_data=back.sh_data.data.numpy(), radius=back.radius.numpy(), center=back.center.numpy(),
-        basis_dim=back.basis_dim, src_density=grid.density_data.data.numpy(), src_sh=grid.sh_data.data.numpy())
+        basis_dim=back.basis_dim, src_density=grid.density_data.data.numpy(), src_sh=grid.sh_data.data.numpy(),
+        **extra)
     print(name, "checkpoint voxels", N)
+
+
+def sparsify_background_case(svox2, name, nlayers, bg_reso, sigma_thresh, seed):
+    """SparseGrid.sparsify_background (svox2/svox2.py:1426-1448) without dilation (the dilation
+    calls the CUDA extension): the background links and data before and after."""
+    gen = torch.Generator().manual_seed(seed)
+    grid = svox2.SparseGrid(reso=4, basis_dim=1, background_nlayers=nlayers, background_reso=bg_reso, device="cpu")
+    bkeep = torch.rand(grid.background_links.shape, generator=gen) >= 0.3
+    bl = torch.full(grid.background_links.shape, -1, dtype=torch.int32)
+    bl[bkeep] = torch.arange(int(bkeep.sum()), dtype=torch.int32)
+    grid.background_links = bl.clone()   # sparsify_background edits the links in place
+    bd = torch.randn((int(bkeep.sum()), nlayers, 4), generator=gen)
+    bd[..., 3] = torch.rand((int(bkeep.sum()), nlayers), generator=gen) * 2.0
+    grid.background_data = torch.nn.Parameter(bd.clone())
+    grid.sparsify_background(sigma_thresh=sigma_thresh, dilate=0)
+    np.savez_compressed(OUT / f"sparsify_bg_{name}.npz", links_in=bl.numpy(), data_in=bd.numpy(),
+                        sigma_thresh=sigma_thresh, links_out=grid.background_links.numpy(),
+                        data_out=grid.background_data.data.numpy())
+    print(name, "background cells", int(bkeep.sum()), "->", int(grid.background_data.shape[0]))
 
 
 def resample_case(svox2, name, reso, new_reso, occupancy, sigma_thresh, seed):
@@ -177,6 +257,11 @@ def main(ref_root: str):
     checkpoint_case(svox2, "sparse10x12x14_sh9", (10, 12, 14), 9, 0.4, [1.2, 0.8, 1.0], [0.1, -0.2, 0.3], 16)
     resample_case(svox2, "sparse12_to_9x14x11", 12, [9, 14, 11], 0.5, 4.0, 17)
     l2_case(svox2, "dense6_sh9", 18)
+    background_case(svox2, "dense8_sh4_l4_r6", 8, 4, 4, 6, 40, 1.0, 0.5, 19)
+    background_case(svox2, "dense6_sh1_l3_r5", 6, 1, 3, 5, 40, 0.5, 0.7, 20)
+    checkpoint_case(svox2, "bg_sparse6x5x4_sh4_l3_r4", (6, 5, 4), 4, 0.5, [1.0, 1.1, 0.9], [0.0, 0.1, 0.0], 21,
+                    bg=(3, 4))
+    sparsify_background_case(svox2, "l4_r6", 4, 6, 1.5, 22)
 
 
 if __name__ == "__main__":

@@ -70,3 +70,40 @@ def test_new_entry_points_validate_on_the_host():
     for call, status, word in cases:
         assert call() == status, lib.svx_last_error()
         assert word in lib.svx_last_error()
+
+
+def test_background_grids_are_validated_on_the_host():
+    """A grid with the MSI background: layer count, null tables, alignment and resolution are
+    checked before any CUDA call (the pointers below are never dereferenced)."""
+    import ctypes as C
+    from svox2_gb300 import _lib
+    lib = _lib.load()
+
+    def grid(**kw):
+        g = _lib.SvxGrid()
+        g.density_data = g.sh_data = g.links = 0x1000
+        g.n_voxels = 64
+        g.size = (C.c_int32 * 3)(4, 4, 4)
+        g.basis_dim, g.sh_data_dim, g.basis_type, g.sh_dtype = 1, 3, 1, _lib.SVX_F32
+        g.background_nlayers, g.background_links, g.background_data = 3, 0x2000, 0x3000
+        g.background_capacity, g.background_reso = 32, 4
+        for k, v in kw.items():
+            setattr(g, k, v)
+        return g
+
+    rays = _lib.SvxRays(0x4000, 0x5000, 0)   # no rays: a valid grid returns before any launch
+    opt = _lib.SvxRenderOpts(1.0, 0.5, 1e-10, 1e-7, 0.0, 0, 0)
+    assert lib.svx_volume_render_cuvol(C.byref(grid()), C.byref(rays), C.byref(opt), None, None, None) == 0
+    rays1 = _lib.SvxRays(0x4000, 0x5000, 1)
+    for kw, word in [({"background_nlayers": 1}, b"layers"), ({"background_data": None}, b"null"),
+                     ({"background_data": 0x3004}, b"aligned"), ({"background_reso": 0}, b"background_reso"),
+                     ({"background_capacity": -1}, b"capacity")]:
+        rc = lib.svx_volume_render_cuvol(C.byref(grid(**kw)), C.byref(rays1), C.byref(opt), 0x6000, None, None)
+        assert rc == _lib.SVX_ERR_INVALID, (kw, lib.svx_last_error())
+        assert word in lib.svx_last_error(), (kw, lib.svx_last_error())
+    rc = lib.svx_msi_tv_grad_sparse(None, 4, None, 32, 3, 4, None, 8, None, C.c_float(1.0), C.c_float(1.0), None,
+                                    None)
+    assert rc == _lib.SVX_ERR_INVALID and b"null" in lib.svx_last_error()
+    rc = lib.svx_msi_tv_grad_sparse(0x1000, 0, 0x2000, 32, 3, 4, 0x3000, 8, None, C.c_float(1.0), C.c_float(1.0),
+                                    0x4000, None)
+    assert rc == _lib.SVX_ERR_INVALID and b"reso" in lib.svx_last_error()

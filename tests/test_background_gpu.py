@@ -1,0 +1,276 @@
+"""MSI background model on the GPU against the CPU oracle (CUDA semantics,
+render_lerp_kernel_cuvol.cu:386-607 and 775-860), through the reference-facing
+operator API: forward, fused MSE adjoint, plain backward, image render, the MSI
+TV gradient, the background optimiser step, sparsify_background with dilation,
+and the SparseGrid autograd path.
+
+Tolerances.  Colours within 5e-5 of the float64 oracle (the background's
+equirectangular map goes through asinf / atan2f, whose last bits differ from
+the host's).  Gradients within 1e-3 relative + 1e-4 of the largest entry of the
+float64 oracle's (scattered with atomics in a different order).  Masks: exactly
+the oracle's where no sample of the ray sits at the early-stop threshold (stop
+threshold 0), else at most 1 % of the rows differ."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+from svox2_gb300 import synthetic as S
+
+from helpers import grid_pair, opt_struct, rays_pair
+
+pytestmark = pytest.mark.gpu
+
+ATOL_RGB = 5e-5
+RTOL_G, ATOL_G_FRAC = 1e-3, 1e-4
+
+
+def _bg_tables(bg_reso, nl, seed, drop=0.2, sigma_scale=4.0):
+    gen = torch.Generator().manual_seed(seed)
+    keep = torch.rand((2 * bg_reso, bg_reso), generator=gen) >= drop
+    links = torch.full(keep.shape, -1, dtype=torch.int32)
+    links[keep] = torch.arange(int(keep.sum()), dtype=torch.int32)
+    data = torch.randn((int(keep.sum()), nl, 4), generator=gen) * 0.5
+    data[..., 3] = torch.rand((int(keep.sum()), nl), generator=gen) * sigma_scale - 0.5
+    return links, data
+
+
+def _case(reso=24, occupancy=0.3, basis_dim=9, nl=8, bg_reso=16, n=600, seed=0, sh_dtype=torch.float32):
+    g = S.make_grid(reso, occupancy=occupancy, basis_dim=basis_dim, seed=seed)
+    spec, og = grid_pair(g, basis_dim=basis_dim, sh_dtype=sh_dtype)
+    bl, bd = _bg_tables(bg_reso, nl, seed + 1)
+    spec.background_links = bl.cuda()
+    spec.background_data = bd.cuda()
+    og.bg_links = bl.numpy()
+    og.bg_data = bd.numpy()
+    o, d, gt = S.make_rays(n, seed=seed + 2)
+    gen = torch.Generator().manual_seed(seed + 3)
+    dr = torch.randn((n // 2, 3), generator=gen)
+    d[n // 2:] = dr / dr.norm(dim=-1, keepdim=True)      # half of the rays in random directions
+    return spec, og, o.contiguous(), d.contiguous(), gt
+
+
+def _grads(C, spec, og, with_mask=True):
+    N = og.density.shape[0]
+    g = C.GridOutputGrads()
+    g.grad_density_out = torch.zeros((N, 1), device="cuda")
+    g.grad_sh_out = torch.zeros((N, og.sh.shape[1]), device="cuda")
+    g.grad_background_out = torch.zeros(spec.background_data.shape, device="cuda")
+    if with_mask:
+        g.mask_out = torch.zeros((N,), dtype=torch.bool, device="cuda")
+        g.mask_background_out = torch.zeros(spec.background_data.shape[:2], dtype=torch.bool, device="cuda")
+    return g
+
+
+def _close_rgb(k, ref, what):
+    err = np.abs(np.asarray(k, np.float64) - ref).max()
+    assert err <= ATOL_RGB, f"{what}: colour error {err:.3e}"
+
+
+def _close_grad(k, ref, what):
+    k = np.asarray(k, np.float64)
+    scale = max(np.abs(ref).max(), 1e-30)
+    bad = np.abs(k - ref) > RTOL_G * np.abs(ref) + ATOL_G_FRAC * scale
+    assert not bad.any(), f"{what}: {bad.sum()} of {bad.size} entries off, max err {np.abs(k - ref).max():.3e}"
+
+
+def _mask_match(k, ref, exact, what):
+    diff = int((np.asarray(k) != ref).sum())
+    limit = 0 if exact else max(1, ref.size // 100)
+    assert diff <= limit, f"{what}: {diff} mask entries differ"
+
+
+@pytest.mark.parametrize("stop", [0.0, 1e-7])
+@pytest.mark.parametrize("basis_dim,sh_dtype", [(9, torch.float32), (4, torch.float32), (9, torch.bfloat16)])
+def test_background_render_and_fused_match_oracle(stop, basis_dim, sh_dtype):
+    from svox2_gb300 import csrc as C
+    spec, og, o, d, gt = _case(basis_dim=basis_dim, sh_dtype=sh_dtype, seed=3)
+    opt, oopt = opt_struct(sigma_thresh=1e-8, stop_thresh=stop, bg=0.7)
+    rays = rays_pair(o, d)
+    # forward
+    rgb = C.volume_render_cuvol(spec, rays, opt)
+    ref0 = O.render(og, oopt, o.numpy(), d.numpy(), mode=0, prec="f64")
+    _close_rgb(rgb.cpu().numpy(), ref0["rgb"], "forward")
+    # the background shows: rays that miss the grid differ from the plain brightness
+    assert np.abs(ref0["rgb"] - 0.7).max() > 0.05
+    # fused
+    out = torch.zeros_like(o, device="cuda")
+    grads = _grads(C, spec, og)
+    C.volume_render_cuvol_fused(spec, rays, opt, gt.cuda(), 0.0, 0.0, out, grads)
+    torch.cuda.synchronize()
+    ref = O.render(og, oopt, o.numpy(), d.numpy(), mode=1, rgb_gt=gt.numpy(), prec="f64")
+    _close_rgb(out.cpu().numpy(), ref["rgb"], "fused colour")
+    _close_grad(grads.grad_density_out.cpu().numpy(), ref["grad_density"], "grad_density")
+    _close_grad(grads.grad_sh_out.cpu().numpy(), ref["grad_sh"], "grad_sh")
+    _close_grad(grads.grad_background_out.cpu().numpy(), ref["grad_background"], "grad_background")
+    assert np.abs(ref["grad_background"]).max() > 0
+    _mask_match(grads.mask_out.cpu().numpy(), ref["mask"], stop == 0.0, "mask")
+    _mask_match(grads.mask_background_out.cpu().numpy(), ref["mask_background"], stop == 0.0, "mask_background")
+
+
+def test_background_fused_sparsity_and_beta_match_oracle():
+    from svox2_gb300 import csrc as C
+    spec, og, o, d, gt = _case(seed=7, n=400)
+    opt, oopt = opt_struct(sigma_thresh=1e-8, stop_thresh=0.0, bg=1.0)
+    out = torch.zeros_like(o, device="cuda")
+    grads = _grads(C, spec, og)
+    C.volume_render_cuvol_fused(spec, rays_pair(o, d), opt, gt.cuda(), 0.05, 0.01, out, grads)
+    torch.cuda.synchronize()
+    ref = O.render(og, oopt, o.numpy(), d.numpy(), mode=1, rgb_gt=gt.numpy(), beta_loss=0.05, sparsity_loss=0.01,
+                   prec="f64")
+    _close_rgb(out.cpu().numpy(), ref["rgb"], "colour")
+    _close_grad(grads.grad_density_out.cpu().numpy(), ref["grad_density"], "grad_density")
+    _close_grad(grads.grad_background_out.cpu().numpy(), ref["grad_background"], "grad_background")
+
+
+def test_background_large_batch_matches_oracle():
+    """40,000 rays: the coherence-sorted order and the padded gradient table of the foreground,
+    the background's vector atomics in between."""
+    from svox2_gb300 import csrc as C
+    spec, og, o, d, gt = _case(reso=32, n=40000, seed=11, nl=6, bg_reso=24)
+    opt, oopt = opt_struct(sigma_thresh=1e-8, stop_thresh=1e-7, bg=1.0)
+    out = torch.zeros_like(o, device="cuda")
+    grads = _grads(C, spec, og)
+    C.volume_render_cuvol_fused(spec, rays_pair(o, d), opt, gt.cuda(), 0.0, 0.0, out, grads)
+    torch.cuda.synchronize()
+    ref = O.render(og, oopt, o.numpy(), d.numpy(), mode=1, rgb_gt=gt.numpy(), prec="f64")
+    _close_rgb(out.cpu().numpy(), ref["rgb"], "colour")
+    _close_grad(grads.grad_density_out.cpu().numpy(), ref["grad_density"], "grad_density")
+    _close_grad(grads.grad_sh_out.cpu().numpy(), ref["grad_sh"], "grad_sh")
+    _close_grad(grads.grad_background_out.cpu().numpy(), ref["grad_background"], "grad_background")
+
+
+def test_background_plain_backward_matches_oracle():
+    from svox2_gb300 import csrc as C
+    spec, og, o, d, gt = _case(seed=13, n=500)
+    opt, oopt = opt_struct(sigma_thresh=1e-8, stop_thresh=1e-7, bg=0.5)
+    rays = rays_pair(o, d)
+    rgb = C.volume_render_cuvol(spec, rays, opt)
+    go = torch.randn(o.shape, generator=torch.Generator().manual_seed(5)) * 0.01
+    grads = _grads(C, spec, og, with_mask=False)
+    C.volume_render_cuvol_backward(spec, rays, opt, go.cuda(), rgb, grads)
+    torch.cuda.synchronize()
+    ref0 = O.render(og, oopt, o.numpy(), d.numpy(), mode=0, prec="f64")
+    ref = O.render(og, oopt, o.numpy(), d.numpy(), mode=2, grad_out=go.numpy(), color=ref0["rgb"], prec="f64")
+    _close_grad(grads.grad_density_out.cpu().numpy(), ref["grad_density"], "grad_density")
+    _close_grad(grads.grad_sh_out.cpu().numpy(), ref["grad_sh"], "grad_sh")
+    _close_grad(grads.grad_background_out.cpu().numpy(), ref["grad_background"], "grad_background")
+
+
+def test_background_image_matches_oracle():
+    from svox2_gb300 import csrc as C
+    spec, og, *_ = _case(seed=17, n=2)
+    opt, oopt = opt_struct(sigma_thresh=1e-8, stop_thresh=1e-7, bg=1.0)
+    c2w = S.look_at_c2w((1.6, 0.9, -1.4))
+    cam = C.CameraSpec()
+    cam.c2w = c2w.cuda()
+    cam.fx = cam.fy = 40.0
+    cam.cx, cam.cy = 32.0, 24.0
+    cam.width, cam.height = 64, 48
+    img = C.volume_render_cuvol_image(spec, cam, opt)
+    ref = O.render_image(og, oopt, c2w.numpy(), 40.0, 40.0, 32.0, 24.0, 64, 48, prec="f64")
+    _close_rgb(img.cpu().numpy(), ref["rgb"], "image")
+
+
+def test_msi_tv_grad_sparse_matches_oracle():
+    from svox2_gb300 import csrc as C
+    bl, bd = _bg_tables(12, 5, seed=21)
+    n_cells = 2 * 12 * 12 * 5
+    cells = torch.randint(0, n_cells, (700,), generator=torch.Generator().manual_seed(2), dtype=torch.int32)
+    grad = torch.zeros_like(bd).cuda()
+    mask = torch.zeros(bd.shape[:2], dtype=torch.bool, device="cuda")
+    C.msi_tv_grad_sparse(bl.cuda(), bd.cuda(), cells.cuda(), mask, 0.3, 0.05, grad)
+    torch.cuda.synchronize()
+    gm = np.zeros(bd.shape[:2], dtype=np.uint8)
+    ref = O.msi_tv_grad(bl.numpy(), bd.numpy(), cells.numpy(), 0.3, 0.05, mask=gm, prec="f64")
+    _close_grad(grad.cpu().numpy(), ref, "msi tv")
+    np.testing.assert_array_equal(mask.cpu().numpy(), gm.astype(bool))
+
+
+@pytest.mark.parametrize("optim", ["rmsprop", "sgd"])
+def test_background_fused_then_optimiser_step(optim):
+    """SparseGrid.volume_render_fused fills the background gradient and its touched-row mask;
+    optim_background_step then updates exactly those rows, sigma at lr_sigma."""
+    import svox2_gb300 as svox2
+    grid = svox2.SparseGrid(reso=16, basis_dim=4, background_nlayers=4, background_reso=8, device="cuda")
+    g = S.make_grid(16, basis_dim=4, seed=4)
+    grid.density_data.data[:] = g.density.cuda() * 0.05
+    grid.sh_data.data[:] = g.sh.cuda()
+    _, bd = _bg_tables(8, 4, seed=5, drop=0.0)
+    grid.background_data.data[:] = bd.cuda()
+    o, d, gt = S.make_rays(300, seed=6)
+    grid.volume_render_fused(svox2.Rays(o.cuda(), d.cuda()), gt.cuda())
+    gb = grid.background_data.grad.clone()
+    mask = grid.sparse_background_indexer.clone()
+    assert mask.any() and gb.abs().max() > 0
+    before = grid.background_data.data.clone()
+    grid.optim_background_step(lr_sigma=2.0, lr_color=0.5, optim=optim)
+    torch.cuda.synchronize()
+    data_ref, _, _ = O.optim(optim == "rmsprop", before.view(-1, 4).cpu().numpy(),
+                             np.zeros((before.numel() // 4, 4), np.float32) if optim == "rmsprop" else None,
+                             gb.view(-1, 4).cpu().numpy(), 2, mask.view(-1).cpu().numpy(), beta=0.9, lr=0.5,
+                             eps=1e-8, lr_last=2.0)
+    np.testing.assert_allclose(grid.background_data.data.view(-1, 4).cpu().numpy(), data_ref, rtol=1e-6, atol=1e-6)
+    untouched = ~mask.view(-1).cpu().numpy()
+    np.testing.assert_array_equal(grid.background_data.data.view(-1, 4).cpu().numpy()[untouched],
+                                  before.view(-1, 4).cpu().numpy()[untouched])
+
+
+def test_background_autograd_matches_fused():
+    """volume_render (autograd, the plain backward) and volume_render_fused give the same
+    background gradient for the MSE loss."""
+    import svox2_gb300 as svox2
+    torch.manual_seed(0)
+    grid = svox2.SparseGrid(reso=16, basis_dim=9, background_nlayers=3, background_reso=6, device="cuda")
+    g = S.make_grid(16, basis_dim=9, seed=8)
+    grid.density_data.data[:] = g.density.cuda() * 0.05
+    grid.sh_data.data[:] = g.sh.cuda()
+    _, bd = _bg_tables(6, 3, seed=9, drop=0.0)
+    grid.background_data.data[:] = bd.cuda()
+    grid.opt.stop_thresh = 0.0
+    o, d, gt = S.make_rays(256, seed=10)
+    rays = svox2.Rays(o.cuda(), d.cuda())
+    rgb = grid.volume_render(rays)
+    torch.nn.functional.mse_loss(rgb, gt.cuda()).backward()
+    g_auto = [grid.density_data.grad.clone(), grid.sh_data.grad.clone(), grid.background_data.grad.clone()]
+    for p in (grid.density_data, grid.sh_data, grid.background_data):
+        p.grad = None
+    rgb2 = grid.volume_render_fused(rays, gt.cuda())
+    torch.testing.assert_close(rgb2, rgb.detach(), rtol=1e-6, atol=1e-6)
+    for a, b in zip(g_auto, (grid.density_data.grad, grid.sh_data.grad, grid.background_data.grad)):
+        scale = float(b.abs().max())
+        assert scale > 0
+        assert float((a - b).abs().max()) <= 1e-4 * scale
+
+
+def test_sparsify_background_with_dilation():
+    """sparsify_background (svox2/svox2.py:1426-1448) with a 3x3x3 dilation of the kept
+    (cell, layer) mask, against a numpy restatement of the same steps."""
+    import svox2_gb300 as svox2
+    grid = svox2.SparseGrid(reso=4, basis_dim=1, background_nlayers=5, background_reso=8, device="cuda")
+    bl, bd = _bg_tables(8, 5, seed=12, drop=0.3, sigma_scale=2.0)
+    grid.background_links = bl.cuda()
+    grid.background_data = torch.nn.Parameter(bd.cuda())
+    grid.sparsify_background(sigma_thresh=1.4, dilate=1)
+    links = bl.numpy()
+    nonempty = links.reshape(-1) >= 0
+    m = np.zeros((links.size, 5), bool)
+    m[nonempty] = bd.numpy()[..., 3] >= 1.4
+    m = O.dilate(m.reshape(links.shape + (5,))).any(-1) & nonempty.reshape(links.shape)
+    new_links = links.copy()
+    new_links[~m] = -1
+    retain = links[m]
+    new_links[m] = np.arange(retain.size, dtype=np.int32)
+    np.testing.assert_array_equal(grid.background_links.cpu().numpy(), new_links)
+    np.testing.assert_array_equal(grid.background_data.data.cpu().numpy(), bd.numpy()[retain])
+
+
+def test_load_checkpoint_with_background_to_cuda_and_render():
+    import svox2_gb300 as svox2
+    from pathlib import Path
+    ckpt = Path(__file__).resolve().parent / "golden" / "ckpt_bg_sparse6x5x4_sh4_l3_r4.npz"
+    grid = svox2.SparseGrid.load(str(ckpt), device="cuda")
+    assert grid.use_background and grid.background_links.is_cuda
+    o, d, _ = S.make_rays(64, seed=1)
+    rgb = grid.volume_render(svox2.Rays(o.cuda(), d.cuda()))
+    assert torch.isfinite(rgb).all()

@@ -388,6 +388,100 @@ def run_render(args):
     print(json.dumps(line), flush=True)
 
 
+def run_background(args):
+    """Training step with the MSI background model at the T&T configuration (64 layers,
+    equirectangular 2048 x 1024 cells, 2.1 GB of background table) on the 256^3 workload:
+    fused render + MSE adjoint with the background composited and differentiated in the same
+    kernel, density / SH / background TV, RMSprop on all three.  Half of the rays leave the
+    grid in random directions (a camera that sees the sky).  Reports rays/s, the same step on
+    the same rays without the background, and the march kernel's roofline: 3648 B per evaluated
+    foreground sample + 48 B per ray + 552 B per background sample (the sample's four corner
+    links and 2 x 4 corner-layer rows gathered twice, 16 B per row, and the rows' gradients read,
+    added and written with their two mask bytes)."""
+    from svox2_gb300 import Rays, SparseGrid
+    from svox2_gb300 import synthetic as S
+    from svox2_gb300 import csrc as C
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    q = args.rays
+    g = S.make_grid(RESO, occupancy=OCC, n_balls=N_BALLS, seed=0, device=dev)
+    o, d, gt = S.make_rays(q, seed=2000)
+    gen = torch.Generator().manual_seed(2001)
+    dr = torch.randn((q // 2, 3), generator=gen)
+    d[q // 2:] = dr / dr.norm(dim=-1, keepdim=True)
+    o, d, gt = o.to(dev), d.to(dev), gt.to(dev)
+    nl, bg_reso = args.bg_layers, args.bg_reso
+    peak, peak_kind = _peaks()
+    res = {}
+    for name, with_bg in (("background", True), ("no_background", False)):
+        grid = SparseGrid.from_tables(g.links.to(dev), g.density.to(dev), g.sh.to(dev))
+        grid.opt.sigma_thresh, grid.opt.stop_thresh = 1e-8, 1e-7
+        if with_bg:
+            grid.background_nlayers, grid.background_reso = nl, bg_reso
+            grid.background_links = torch.arange(2 * bg_reso * bg_reso, dtype=torch.int32,
+                                                  device=dev).view(2 * bg_reso, bg_reso)
+            bgd = torch.randn((2 * bg_reso * bg_reso, nl, 4), generator=torch.Generator(device=dev).manual_seed(3),
+                              device=dev) * 0.3
+            bgd[..., 3] = 0.1          # the reference's init_sigma_bg
+            grid.background_data = torch.nn.Parameter(bgd)
+        rays = Rays(o, d)
+
+        def step():
+            grid.volume_render_fused(rays, gt)
+            grid.inplace_tv_grad(grid.density_data.grad, scaling=5e-5, sparse_frac=0.01, contiguous=True)
+            grid.inplace_tv_color_grad(grid.sh_data.grad, scaling=5e-3, sparse_frac=0.01, contiguous=True)
+            if with_bg:
+                grid.inplace_tv_background_grad(grid.background_data.grad, scaling=1e-3, scaling_density=1e-3,
+                                                sparse_frac=0.01, contiguous=True)
+            grid.optim_density_step(30.0, beta=0.95)
+            grid.optim_sh_step(1e-2, beta=0.95)
+            if with_bg:
+                grid.optim_background_step(3.0, 0.1, beta=0.95)
+
+        for _ in range(max(args.warmup, 3)):
+            step()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            step()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        # the march kernel alone, with its sample counts
+        st = {"eval_samples": torch.zeros(1, dtype=torch.int64, device=dev),
+              "background_samples": torch.zeros(1, dtype=torch.int64, device=dev),
+              "march_start": torch.cuda.Event(enable_timing=True),
+              "march_stop": torch.cuda.Event(enable_timing=True)}
+        holder = C.GridOutputGrads()
+        gd, gs = grid._get_data_grads()
+        holder.grad_density_out, holder.grad_sh_out = gd, gs
+        if with_bg:
+            holder.grad_background_out = grid._grad_buffer(grid.background_data)
+        r = C.RaysSpec()
+        r.origins, r.dirs = o, d
+        out = torch.empty_like(gt)
+        C.volume_render_cuvol_fused(grid._to_cpp(), r, grid.opt._to_cpp(), gt, 0.0, 0.0, out, holder, stats=st)
+        torch.cuda.synchronize()
+        kms = st["march_start"].elapsed_time(st["march_stop"])
+        n_fg, n_bg = int(st["eval_samples"].item()), int(st["background_samples"].item())
+        achieved = (3648 * n_fg + 48 * q + 552 * n_bg) / (kms / 1e3) / 1e9
+        res[name] = {"rays_per_s": q / (ms / 1e3), "ms_per_step": ms, "kernel_ms": kms, "eval_samples": n_fg,
+                     "background_samples": n_bg,
+                     "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                                  "frac": achieved / peak, "peak_kind": peak_kind}}
+        del grid
+        torch.cuda.empty_cache()
+    line = {"metric": f"fused fwd+bwd rays/s at 256^3 SH9 with the MSI background ({nl} layers, {bg_reso} reso)",
+            "unit": "rays/s", "value": res["background"]["rays_per_s"], "steps": args.steps, "dtype": "f32",
+            "data": "synthetic", "higher_is_better": True,
+            "config": {"workload": f"train step 256^3 20% occupancy SH9 FP32 + MSI background {nl} x {2 * bg_reso} x {bg_reso}, "
+                                   f"{q} rays per step, half leaving the grid in random directions"},
+            "roofline": res["background"]["roofline"], "results": res}
+    print(json.dumps(line), flush=True)
+
+
 def run_serve(args):
     """Serving configuration: a Poisson stream (2000 requests/s) of render requests (square
     images, side U{64..800}, cameras on a radius-4 sphere looking at the origin) and train-step
@@ -503,11 +597,14 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--rays", type=int, default=1_000_000, help="rays per step (profiling runs use a smaller case)")
     ap.add_argument("--skip-e2e", action="store_true", help="leave out the host-copy arm (profiling runs)")
-    ap.add_argument("--config", default="train", choices=["train", "mixed", "serve", "render"],
+    ap.add_argument("--config", default="train", choices=["train", "mixed", "serve", "render", "background"],
                     help="train: the 256^3 training step (default); mixed: 512^3 BF16/FP16 SH vs FP32; "
                          "serve: continuous-batching server vs serial launches; "
-                         "render: forward-only render of the 256^3 workload, FP32 and BF16 SH")
+                         "render: forward-only render of the 256^3 workload, FP32 and BF16 SH; "
+                         "background: the training step with the T&T MSI background")
     ap.add_argument("--requests", type=int, default=600, help="serve: number of requests in the stream")
+    ap.add_argument("--bg-layers", type=int, default=64, help="background: MSI layers (the T&T configuration's 64)")
+    ap.add_argument("--bg-reso", type=int, default=1024, help="background: MSI resolution (T&T: 1024)")
     ap.add_argument("--rate", type=float, default=2000.0, help="serve: Poisson arrival rate (requests/s)")
     args = ap.parse_args()
     if args.config == "mixed":
@@ -518,6 +615,9 @@ def main():
         return
     if args.config == "render":
         run_render(args)
+        return
+    if args.config == "background":
+        run_background(args)
         return
     Q = args.rays
     args.warmup = max(args.warmup, 3)

@@ -138,12 +138,15 @@ typedef struct {
  *                 cudaEvent_t handles of the caller (or NULL), recorded on the
  *                 call's stream just before and just after the ray-march kernel,
  *                 so that its duration can be told apart from the ray sort and
- *                 the gradient flush around it. */
+ *                 the gradient flush around it.
+ *   background_samples  device uint64 accumulator: += number of MSI background
+ *                 samples (sigma > 0, before early stop) over the launch. */
 typedef struct {
   uint64_t* eval_samples;
   uint64_t* ray_trace;
   void* march_start;
   void* march_stop;
+  uint64_t* background_samples;
 } svx_render_stats_t;
 
 /* ---- rendering: svox2/csrc/render_lerp_kernel_cuvol.cu ---------------- */

@@ -129,6 +129,7 @@ def render(grid: Grid, opt: Opt, origins, dirs, mode: int = 0, rgb_gt=None, grad
     mask = np.zeros((N,), dtype=np.uint8) if (mode == 1 and want_mask) else None
     tr = np.zeros((Q,), dtype=np.uint64) if trace else None
     ne = np.zeros((1,), dtype=np.uint64)
+    nb = np.zeros((1,), dtype=np.uint64)
     has_bg = grid.bg_links is not None and grid.bg_links.size > 0
     gbg = np.zeros(grid.bg_data.shape, dtype=R) if (has_bg and mode and want_grads) else None
     mbg = np.zeros(grid.bg_data.shape[:2], dtype=np.uint8) if (has_bg and mode == 1 and want_mask) else None
@@ -141,10 +142,11 @@ def render(grid: Grid, opt: Opt, origins, dirs, mode: int = 0, rgb_gt=None, grad
     fn(C.byref(g), C.byref(o), C.c_void_p(_p(origins)), C.c_void_p(_p(dirs)), C.c_int64(Q), C.c_int(mode),
        C.c_void_p(_p(gt)), C.c_void_p(_p(go)), C.c_float(beta_loss), C.c_float(sparsity_loss),
        C.c_void_p(_p(rgb)), C.c_void_p(_p(gd)), C.c_void_p(_p(gs)), C.c_void_p(_p(mask)), C.c_void_p(_p(gbg)),
-       C.c_void_p(_p(mbg)), C.c_void_p(_p(tr)), C.c_void_p(_p(ne)), C.c_int(nthreads or default_threads()))
+       C.c_void_p(_p(mbg)), C.c_void_p(_p(tr)), C.c_void_p(_p(ne)), C.c_void_p(_p(nb)),
+       C.c_int(nthreads or default_threads()))
     return {"rgb": rgb, "grad_density": gd, "grad_sh": gs, "mask": None if mask is None else mask.astype(bool),
             "grad_background": gbg, "mask_background": None if mbg is None else mbg.astype(bool),
-            "trace": tr, "n_eval": int(ne[0])}
+            "trace": tr, "n_eval": int(ne[0]), "n_background": int(nb[0])}
 
 
 def render_image(grid: Grid, opt: Opt, c2w, fx, fy, cx, cy, width, height, ndc=(-1.0, -1.0), prec="f32",

@@ -460,7 +460,7 @@ static void FN(bg_scatter)(const oracle_grid_t* g, const int l[3], const REAL po
  * grad_bg / mask_bg. */
 static void FN(bg_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const REAL org[3], const REAL dir[3],
                        REAL lt, const REAL* gout, REAL accum, REAL sparsity, REAL out[3], REAL* grad_bg,
-                       uint8_t* mask_bg) {
+                       uint8_t* mask_bg, uint64_t* n_samples) {
   const REAL C0 = (REAL)0.28209479177387814f;
   const int nl = g->bg_nlayers, cpu = opt->bg_cpu;
   const REAL log_stop = cpu ? (REAL)(-INFINITY) : FN(log_stop)(opt->stop_thresh);
@@ -503,6 +503,7 @@ static void FN(bg_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const RE
       const REAL pcnt = cpu ? b.ws * sigma * width : width * b.ws * sigma;
       const REAL w = EXP(lt) * ((REAL)1 - EXP(-pcnt));
       lt = lt - pcnt;
+      if (n_samples) ++*n_samples;
       if (gout == NULL) {
         for (c = 0; c < 3; ++c) outv[c] = outv[c] + w * FMAX(FN(bg_trilerp)(g, l, pos, c) * C0 + (REAL)0.5, (REAL)0);
       } else {
@@ -575,16 +576,17 @@ void FN(oracle_msi_tv_grad)(const int32_t* links, int size0, int size1, const fl
 void FN(oracle_render)(const oracle_grid_t* g, const oracle_opt_t* opt, const float* origins, const float* dirs,
                        int64_t Q, int mode, const float* rgb_gt, const float* grad_out, float beta_loss,
                        float sparsity, REAL* rgb_out, REAL* grad_density, REAL* grad_sh, uint8_t* mask,
-                       REAL* grad_bg, uint8_t* mask_bg, uint64_t* trace, uint64_t* n_eval_total, int nthreads) {
+                       REAL* grad_bg, uint8_t* mask_bg, uint64_t* trace, uint64_t* n_eval_total,
+                       uint64_t* n_bg_total, int nthreads) {
   int64_t q;
-  uint64_t total = 0;
+  uint64_t total = 0, total_bg = 0;
   const REAL norm = (REAL)2.f / (REAL)(float)(3 * Q);
   if (nthreads < 1) nthreads = 1;
-#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads) reduction(+ : total)
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads) reduction(+ : total, total_bg)
   for (q = 0; q < Q; ++q) {
     REAL org[3], dir[3], out[3], gout[3], lt = 0, acc_b = 0, lt_b = 0;
     const int bg = g->bg_nlayers > 0;
-    uint64_t ne = 0;
+    uint64_t ne = 0, nb = 0;
     int i;
     for (i = 0; i < 3; ++i) {
       org[i] = (REAL)origins[q * 3 + i];
@@ -593,7 +595,7 @@ void FN(oracle_render)(const oracle_grid_t* g, const oracle_opt_t* opt, const fl
     if (mode == 0 || mode == 1) {
       FN(fwd_ray)(g, opt, org, dir, out, &lt, trace ? trace + q : NULL, &ne);
       /* render_background_kernel skips rays whose log transmittance is below -25 */
-      if (bg && lt >= (REAL)-25) FN(bg_ray)(g, opt, org, dir, lt, NULL, 0, 0, out, NULL, NULL);
+      if (bg && lt >= (REAL)-25) FN(bg_ray)(g, opt, org, dir, lt, NULL, 0, 0, out, NULL, NULL, &nb);
       for (i = 0; i < 3; ++i) rgb_out[q * 3 + i] = out[i];
     }
     if (mode == 1) {
@@ -602,7 +604,7 @@ void FN(oracle_render)(const oracle_grid_t* g, const oracle_opt_t* opt, const fl
                   grad_sh, mask, &acc_b, &lt_b);
       /* the fused path's background backward starts from the forward's log transmittance */
       if (bg && lt >= (REAL)-25)
-        FN(bg_ray)(g, opt, org, dir, lt, gout, acc_b, (REAL)sparsity, NULL, grad_bg, mask_bg);
+        FN(bg_ray)(g, opt, org, dir, lt, gout, acc_b, (REAL)sparsity, NULL, grad_bg, mask_bg, NULL);
     } else if (mode == 2) {
       for (i = 0; i < 3; ++i) {
         out[i] = rgb_out[q * 3 + i];
@@ -610,11 +612,13 @@ void FN(oracle_render)(const oracle_grid_t* g, const oracle_opt_t* opt, const fl
       }
       FN(bwd_ray)(g, opt, org, dir, out, 0, gout, 0, 0, grad_density, grad_sh, NULL, &acc_b, &lt_b);
       /* volume_render_cuvol_backward: from the backward pass's own log transmittance */
-      if (bg && lt_b >= (REAL)-25) FN(bg_ray)(g, opt, org, dir, lt_b, gout, acc_b, 0, NULL, grad_bg, NULL);
+      if (bg && lt_b >= (REAL)-25) FN(bg_ray)(g, opt, org, dir, lt_b, gout, acc_b, 0, NULL, grad_bg, NULL, NULL);
     }
     total += ne;
+    total_bg += nb;
   }
   if (n_eval_total) *n_eval_total += total;
+  if (n_bg_total) *n_bg_total += total_bg;
 }
 
 /* trace_ray_expected_term (render_lerp_kernel_cuvol.cu:122-176) and trace_ray_sigma_thresh
@@ -755,7 +759,7 @@ void FN(oracle_render_image)(const oracle_grid_t* g, const oracle_opt_t* opt, co
     int i;
     FN(camera_ray)((int)(q % cam->width), (int)(q / cam->width), cam, dir, org);
     FN(fwd_ray)(g, opt, org, dir, rgb, &lt, trace ? trace + q : NULL, &ne);
-    if (g->bg_nlayers > 0 && lt >= (REAL)-25) FN(bg_ray)(g, opt, org, dir, lt, NULL, 0, 0, rgb, NULL, NULL);
+    if (g->bg_nlayers > 0 && lt >= (REAL)-25) FN(bg_ray)(g, opt, org, dir, lt, NULL, 0, 0, rgb, NULL, NULL, NULL);
     for (i = 0; i < 3; ++i) out[q * 3 + i] = rgb[i];
   }
 }

@@ -85,7 +85,7 @@ class SvxGridGrads(C.Structure):
 
 class SvxRenderStats(C.Structure):
     _fields_ = [("eval_samples", C.c_void_p), ("ray_trace", C.c_void_p), ("march_start", C.c_void_p),
-                ("march_stop", C.c_void_p)]
+                ("march_stop", C.c_void_p), ("background_samples", C.c_void_p)]
 
 
 class SvxBatchGrid(C.Structure):

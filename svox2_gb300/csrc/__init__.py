@@ -232,6 +232,7 @@ def _stats_struct(stats) -> Optional[C.POINTER(_lib.SvxRenderStats)]:
     s = _lib.SvxRenderStats()
     s.eval_samples = _ptr(stats.get("eval_samples"))
     s.ray_trace = _ptr(stats.get("ray_trace"))
+    s.background_samples = _ptr(stats.get("background_samples"))
     # torch.cuda.Event objects (timing enabled) recorded around the ray-march kernel
     for key in ("march_start", "march_stop"):
         ev = stats.get(key)

@@ -451,6 +451,7 @@ static int render_rays(const svx_grid_t* grid, const svx_rays_t* rays, const svx
   io.n_rays = rays->n_rays;
   io.eval_count = stats ? reinterpret_cast<unsigned long long*>(stats->eval_samples) : nullptr;
   io.trace = stats ? reinterpret_cast<unsigned long long*>(stats->ray_trace) : nullptr;
+  io.bg_eval_count = stats ? reinterpret_cast<unsigned long long*>(stats->background_samples) : nullptr;
   io.cap = g_cap;
   rc = set_background(io, grid, o, nullptr);
   if (rc) return rc;
@@ -576,6 +577,7 @@ extern "C" int svx_volume_render_cuvol_image(const svx_grid_t* grid, const svx_c
   io.rgb_out = rgb_out;
   io.eval_count = stats ? reinterpret_cast<unsigned long long*>(stats->eval_samples) : nullptr;
   io.trace = stats ? reinterpret_cast<unsigned long long*>(stats->ray_trace) : nullptr;
+  io.bg_eval_count = stats ? reinterpret_cast<unsigned long long*>(stats->background_samples) : nullptr;
   io.cap = 0;
   rc = set_background(io, grid, o, nullptr);
   if (rc) return rc;
@@ -679,6 +681,7 @@ extern "C" int svx_volume_render_cuvol_fused_noalloc(const svx_grid_t* grid, con
   io.n_rays = rays->n_rays;
   io.eval_count = stats ? reinterpret_cast<unsigned long long*>(stats->eval_samples) : nullptr;
   io.trace = stats ? reinterpret_cast<unsigned long long*>(stats->ray_trace) : nullptr;
+  io.bg_eval_count = stats ? reinterpret_cast<unsigned long long*>(stats->background_samples) : nullptr;
   io.cap = g_cap;
   rc = set_background(io, grid, o, grads);
   if (rc) return rc;

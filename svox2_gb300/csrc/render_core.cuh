@@ -86,6 +86,7 @@ struct IoP {
   int bg_reso, bg_nl;
   float* grad_bg;              // optional [bg_cap, bg_nl, 4]
   uint8_t* mask_bg;            // optional [bg_cap, bg_nl]
+  unsigned long long* bg_eval_count;  // optional: += background samples
 };
 
 // ---------------------------------------------------------------- per-ray setup
@@ -813,10 +814,13 @@ __device__ __forceinline__ void bg_setup(BgArgs& b, const float org[3], const fl
 }
 
 // Sample of shell i: false when the shell is inside the inner radius or not hit.  Returns 1/r
-// of the sample point, its (x, y, layer) cell and the fractional position in it.
+// of the sample point, its (x, y, layer) cell and the fractional position in it.  The radius
+// n / (n - i - 0.5) is one float division of exact operands (the reference divides in double
+// and rounds to float, which differs only where the quotient sits on a float midpoint), and
+// 1/|p| is rnorm3df, as the reference's _rnorm computes it.
 __device__ __forceinline__ bool bg_sample(const BgArgs& b, int i, float& invr, int l[3], float pos[3]) {
   if (i >= b.n_steps) return false;
-  const float r = (float)__ddiv_rn((double)b.n_steps, __dsub_rn((double)(b.n_steps - i), 0.5));
+  const float r = __fdiv_rn((float)b.n_steps, __fsub_rn((float)(b.n_steps - i), 0.5f));
   if (r < b.inner) return false;
   const float det = __fadd_rn(b.f, __fmul_rn(__fmul_rn(__fmul_rn(2.f, b.q2a), r), r));
   if (det < 0.f) return false;
@@ -824,7 +828,7 @@ __device__ __forceinline__ bool bg_sample(const BgArgs& b, int i, float& invr, i
   float p[3];
 #pragma unroll
   for (int j = 0; j < 3; ++j) p[j] = fmaf(t, b.d[j], b.o[j]);
-  invr = rnorm3_exact(p[0], p[1], p[2]);
+  invr = rnorm3df(p[0], p[1], p[2]);
 #pragma unroll
   for (int j = 0; j < 3; ++j) p[j] = __fmul_rn(p[j], invr);
   // _unitvec2equirect, render_util.cuh:482-490 (its double constants make the arithmetic double).
@@ -930,13 +934,15 @@ __device__ __forceinline__ void bg_chunk(const BgArgs& b, int i0, int lane, floa
   c.em = em;
 }
 
-// Background colour from log transmittance lt, brightness term included (cuvol.cu:386-476).
-static __device__ __noinline__ float3 bg_forward(const BgArgs& b, float lt, int lane) {
+// Background colour from log transmittance lt, brightness term included (cuvol.cu:386-476);
+// adds the number of samples that counted to *n_samples.
+__device__ __forceinline__ float3 bg_forward(const BgArgs& b, float lt, int lane, unsigned* n_samples) {
   float a0 = 0.f, a1 = 0.f, a2 = 0.f;
   float invr_carry = b.invr0;
   for (int i0 = 0; i0 < b.n_steps; i0 += 32) {
     BgChunk c;
     bg_chunk(b, i0, lane, invr_carry, lt, c);
+    *n_samples += __popc(c.em);
     if ((c.em >> lane) & 1u) {
       const float w = sample_weight(c.lt_before, c.pcnt);
       a0 = fmaf(w, fmaxf(__fadd_rn(__fmul_rn(c.v[0], kC0), 0.5f), 0.f), a0);
@@ -959,8 +965,8 @@ static __device__ __noinline__ float3 bg_forward(const BgArgs& b, float lt, int 
 // the background carries; each sample's share w * dot(max(colour, 0), g) comes off it in shell
 // order (a prefix sum over the chunk), and the gradients of the four channels of a corner-layer
 // row go out as one vector atomic.
-static __device__ __noinline__ void bg_backward(const BgArgs& b, float lt, float g0, float g1, float g2, float accum,
-                                         float sparsity, int lane) {
+__device__ __forceinline__ void bg_backward(const BgArgs& b, float lt, float g0, float g1, float g2, float accum,
+                                            float sparsity, int lane) {
   float invr_carry = b.invr0;
   for (int i0 = 0; i0 < b.n_steps; i0 += 32) {
     BgChunk c;
@@ -1036,6 +1042,7 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 5 : 4) render_kernel(
   const long long n_rays = MULTI ? *io.n_rays_dev : io.n_rays;
 
   unsigned long long evals = 0;
+  unsigned bg_evals = 0;   // background samples (grids with the MSI background)
   unsigned long long next = 0;
   if (lane == 0) next = atomicAdd(io.work, 1ull);
   next = __shfl_sync(kFull, next, 0);
@@ -1073,37 +1080,16 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 5 : 4) render_kernel(
     unsigned long long* thp = io.trace != nullptr ? &th : nullptr;
 
     if (!(rg.tmin <= rg.tmax)) {
-      // Ray misses the grid: background only (cuvol.cu:42-48, 253-258).
-      if constexpr (BG) {
-        // the MSI background from full transmittance, and its gradient (cuvol.cu:776-860)
-        BgArgs b;
-        bg_setup(b, org, dir, g, opt, io);
-        const float3 c = bg_forward(b, 0.f, lane);
-        if (MODE != kBwd && lane == 0) {
-          io.rgb_out[ray * 3 + 0] = c.x;
-          io.rgb_out[ray * 3 + 1] = c.y;
-          io.rgb_out[ray * 3 + 2] = c.z;
-        }
-        if (MODE != kFwd) {
-          float q0, q1, q2;
-          if (MODE == kFused) {
-            q0 = __fmul_rn(__fsub_rn(c.x, __ldg(io.rgb_gt + ray * 3 + 0)), go.norm);
-            q1 = __fmul_rn(__fsub_rn(c.y, __ldg(io.rgb_gt + ray * 3 + 1)), go.norm);
-            q2 = __fmul_rn(__fsub_rn(c.z, __ldg(io.rgb_gt + ray * 3 + 2)), go.norm);
-          } else {
-            q0 = __ldg(io.grad_out + ray * 3 + 0);
-            q1 = __ldg(io.grad_out + ray * 3 + 1);
-            q2 = __ldg(io.grad_out + ray * 3 + 2);
-          }
-          const float acc = fmaf(c.x, q0, fmaf(c.y, q1, __fmul_rn(c.z, q2)));
-          bg_backward(b, 0.f, q0, q1, q2, acc, go.sparsity, lane);
-        }
-      } else {
+      if constexpr (!BG) {
+        // Ray misses the grid: background only, no gradient (cuvol.cu:42-48, 253-258).
         if (MODE != kBwd && lane < 3) io.rgb_out[ray * 3 + lane] = opt.bg;
+        if (io.trace != nullptr && lane == 0) io.trace[ray] = th;
+        next = __shfl_sync(kFull, next, 0);
+        continue;
       }
-      if (io.trace != nullptr && lane == 0) io.trace[ray] = th;
-      next = __shfl_sync(kFull, next, 0);
-      continue;
+      // With the MSI background the ray goes on with no foreground: the march below does not
+      // run (t > tmax), and the background is rendered, and differentiated, from full
+      // transmittance (cuvol.cu:42-48 writes 0, the background kernels add to it, 776-860).
     }
 
     // ---- forward march
@@ -1205,7 +1191,7 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 5 : 4) render_kernel(
       tb0 = tb1 = tb2 = 0.f;
       if (with_bg) {
         bg_setup(bga, org, dir, g, opt, io);
-        const float3 c = bg_forward(bga, lt_bg, lane);
+        const float3 c = bg_forward(bga, lt_bg, lane, &bg_evals);
         tb0 = c.x;
         tb1 = c.y;
         tb2 = c.z;
@@ -1406,6 +1392,10 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 5 : 4) render_kernel(
     next = __shfl_sync(kFull, next, 0);
   }
   if (io.eval_count != nullptr && lane == 0 && evals) atomicAdd(io.eval_count, evals);
+  if constexpr (BG) {
+    if (io.bg_eval_count != nullptr && lane == 0 && bg_evals)
+      atomicAdd(io.bg_eval_count, (unsigned long long)bg_evals);
+  }
 }
 
 // colour cache capacity (samples per ray) of the adjoint; defined in render.cu

@@ -231,6 +231,31 @@ def cpu_sample(g, budget_s: float = 12.0, threads: int | None = None):
     return n / t, threads, f"{n} rays of the 256^3 workload fused fwd+bwd + TV/RMSprop on {n}/{Q} of the grid"
 
 
+def bg_cpu_sample(g, bg_links, bg_data, o, d, gt, budget_s: float = 10.0, threads: int | None = None):
+    """The oracle's fused fwd+bwd with the MSI background on a bounded sample of the background
+    workload's rays (the same half-and-half mix).  Returns (rays/s, cores, desc)."""
+    from oracle import oracle as O
+    from svox2_gb300 import synthetic as S
+
+    threads = threads or (os.cpu_count() or 1)
+    off, scl = S.grid_transform(g.reso)
+    og = O.Grid(g.links.numpy(), g.density.numpy(), g.sh.numpy(), 9, off, scl, bg_links=bg_links, bg_data=bg_data)
+    opt = O.Opt(1.0, 0.5, 1e-8, 1e-7)
+    q = o.shape[0]
+
+    def step(n):
+        idx = np.concatenate([np.arange(n // 2), q // 2 + np.arange(n - n // 2)])
+        t0 = time.perf_counter()
+        O.render(og, opt, o[idx], d[idx], mode=1, rgb_gt=gt[idx], nthreads=threads)
+        return time.perf_counter() - t0
+
+    n = 512
+    t = step(n)
+    n = int(max(512, min(q, n * budget_s / max(t, 1e-3))))
+    t = step(n)
+    return n / t, threads, f"{n} rays of the background workload, fused fwd+bwd with the background (no TV/optimiser)"
+
+
 def run_reference(args, rank, world):
     """Reference arm: the CPU restatement of the reference algorithm, all host threads."""
     if rank != 0:
@@ -471,6 +496,11 @@ def run_background(args):
                      "background_samples": n_bg,
                      "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                                   "frac": achieved / peak, "peak_kind": peak_kind}}
+        if with_bg and not args.no_cpu_baseline:
+            v, cores, desc = bg_cpu_sample(g, grid.background_links.cpu().numpy(),
+                                           grid.background_data.data.cpu().numpy(), o.cpu().numpy(),
+                                           d.cpu().numpy(), gt.cpu().numpy())
+            res["cpu_baseline"] = {"value": v, "unit": "rays/s", "cores": cores, "kind": "port", "sample": desc}
         del grid
         torch.cuda.empty_cache()
     line = {"metric": f"fused fwd+bwd rays/s at 256^3 SH9 with the MSI background ({nl} layers, {bg_reso} reso)",
@@ -478,7 +508,8 @@ def run_background(args):
             "data": "synthetic", "higher_is_better": True,
             "config": {"workload": f"train step 256^3 20% occupancy SH9 FP32 + MSI background {nl} x {2 * bg_reso} x {bg_reso}, "
                                    f"{q} rays per step, half leaving the grid in random directions"},
-            "roofline": res["background"]["roofline"], "results": res}
+            "roofline": res["background"]["roofline"], "cpu_baseline": res.pop("cpu_baseline", None),
+            "results": res}
     print(json.dumps(line), flush=True)
 
 

@@ -64,9 +64,9 @@ typedef enum { SVX_F32 = 0, SVX_BF16 = 1, SVX_F16 = 2 } svx_dtype;
  *   background_data   float32 [background_capacity, background_nlayers, 4], 16-byte
  *              aligned: per layer three colour coefficients (scaled by the SH DC
  *              constant) and sigma.  A link >= background_capacity reads as empty.
- * The MSI background is rendered by the ray entry points (cuvol.cu:386-607);
- * svx_render_batch, svx_ray_order and the depth renders ignore it, as the
- * reference's depth renders do. */
+ * The MSI background is rendered by the ray entry points (cuvol.cu:386-607) and by
+ * svx_render_batch when its with_background flag is set; svx_ray_order and the
+ * depth renders ignore it, as the reference's depth renders do. */
 typedef struct {
   const float* density_data;
   const void* sh_data;
@@ -239,7 +239,11 @@ typedef struct {
 
 /* Render (mode 0) or fused-MSE render (mode 1) of a batch of rays.
  *   grids       device array of svx_batch_grid_t; the host does not read it,
- *               so the caller vouches for it (pointers, sizes, basis_dim)
+ *               so the caller vouches for it (pointers, sizes, basis_dim; an
+ *               MSI background's table and gradient 16-byte aligned)
+ *   with_background  0: every grid is rendered without its MSI background
+ *               (a faster kernel); 1: grids whose background_nlayers > 0 are
+ *               rendered, and in mode 1 differentiated, with it
  *   ray_grid    device int32 [max_rays], the grid of each ray
  *   n_rays_dev  device int64: rays processed by this launch (<= max_rays); it
  *               is read on the device, so that a captured CUDA graph of this
@@ -251,7 +255,7 @@ typedef struct {
  *   work        device uint64 scratch of the caller (cleared by the call)
  * Allocates nothing.  max_rays sizes the persistent grid. */
 int svx_render_batch(int32_t mode, const svx_batch_grid_t* grids, int32_t basis_dim, int32_t sh_dtype,
-                     const float* origins, const float* dirs, const int32_t* ray_grid,
+                     int32_t with_background, const float* origins, const float* dirs, const int32_t* ray_grid,
                      const int32_t* order, const int64_t* n_rays_dev, int64_t max_rays,
                      const svx_render_opts_t* opt, const float* rgb_gt, float* rgb_out, uint64_t* work,
                      void* stream);

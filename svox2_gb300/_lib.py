@@ -110,8 +110,8 @@ SIGNATURES = {
                                       P(SvxGridGrads), P(SvxRenderStats), _vp],
     "svx_volume_render_cuvol_fused_noalloc": [P(SvxGrid), P(SvxRays), P(SvxRenderOpts), _vp, _f32, _f32, _vp,
                                               P(SvxGridGrads), P(SvxRenderStats), _vp],
-    "svx_render_batch": [_i32, _vp, _i32, _i32, _vp, _vp, _vp, _vp, _vp, _i64, P(SvxRenderOpts), _vp, _vp, _vp,
-                         _vp],
+    "svx_render_batch": [_i32, _vp, _i32, _i32, _i32, _vp, _vp, _vp, _vp, _vp, _i64, P(SvxRenderOpts), _vp, _vp,
+                         _vp, _vp],
     "svx_ray_order": [P(SvxGrid), P(SvxRays), P(SvxRenderOpts), _i32, _vp, _vp],
     "svx_add_accum": [_vp, _i32, _i32, _i64, _vp, _vp, _vp],
     "svx_camera_rays": [P(SvxCamera), _vp, _vp, _vp],

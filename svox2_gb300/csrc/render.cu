@@ -735,7 +735,7 @@ extern "C" int svx_camera_rays(const svx_camera_t* cam, float* origins, float* d
 }
 
 extern "C" int svx_render_batch(int32_t mode, const svx_batch_grid_t* grids, int32_t basis_dim, int32_t sh_dtype,
-                                const float* origins, const float* dirs, const int32_t* ray_grid,
+                                int32_t with_background, const float* origins, const float* dirs, const int32_t* ray_grid,
                                 const int32_t* order, const int64_t* n_rays_dev, int64_t max_rays,
                                 const svx_render_opts_t* opt, const float* rgb_gt, float* rgb_out, uint64_t* work,
                                 void* stream) {
@@ -764,6 +764,7 @@ extern "C" int svx_render_batch(int32_t mode, const svx_batch_grid_t* grids, int
   io.cap = g_cap;
   GridP g{};  // per-ray grids come from the descriptors
   cudaStream_t st = as_stream(stream);
+  if (with_background) return dispatch_bg_batch(mode == 0 ? kFwd : kFused, sh_dtype, g, o, io, max_rays, st);
   switch (sh_dtype) {
     case SVX_F32:
       return mode == 0 ? launch_t<9, float, kFwd, false, true>(g, o, io, max_rays, st)

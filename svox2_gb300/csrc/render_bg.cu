@@ -1,8 +1,9 @@
 // Render kernel instantiations for grids with the MSI background model
 // (render_lerp_kernel_cuvol.cu:386-607 and 775-860): the ray march of
 // render_core.cuh with the background composited, and differentiated, in the same
-// pass as the foreground.  A translation unit of their own, so that they
-// compile in parallel with render.cu's.
+// pass as the foreground; and the SH9 batch kernels whose grids may carry one.
+// A translation unit of their own, so that they compile in parallel with
+// render.cu's.
 #include "render_core.cuh"
 
 namespace svx {
@@ -16,6 +17,25 @@ int dispatch_bg(int mode, bool image, int bd, int dt, const GridP& g, const OptP
   SVX_REQUIRE(!image, SVX_ERR_INVALID, "image renders are forward only");
   if (mode == kFused) return dispatch_bd<kFused, false, false, true>(bd, dt, g, opt, io, n, st);
   return dispatch_bd<kBwd, false, false, true>(bd, dt, g, opt, io, n, st);
+}
+
+int dispatch_bg_batch(int mode, int dt, const GridP& g, const OptP& opt, const IoP& io, long long n,
+                      cudaStream_t st) {
+  SVX_REQUIRE(mode == kFwd || mode == kFused, SVX_ERR_INVALID, "batch mode %d: render or fused", mode);
+  const bool fwd = mode == kFwd;
+  switch (dt) {
+    case SVX_F32:
+      return fwd ? launch_t<9, float, kFwd, false, true, true>(g, opt, io, n, st)
+                 : launch_t<9, float, kFused, false, true, true>(g, opt, io, n, st);
+    case SVX_BF16:
+      return fwd ? launch_t<9, __nv_bfloat16, kFwd, false, true, true>(g, opt, io, n, st)
+                 : launch_t<9, __nv_bfloat16, kFused, false, true, true>(g, opt, io, n, st);
+    case SVX_F16:
+      return fwd ? launch_t<9, __half, kFwd, false, true, true>(g, opt, io, n, st)
+                 : launch_t<9, __half, kFused, false, true, true>(g, opt, io, n, st);
+  }
+  set_error("sh_dtype %d unknown", dt);
+  return SVX_ERR_INVALID;
 }
 
 }  // namespace rk

@@ -766,18 +766,40 @@ struct BgArgs {
   float q2a, qb, f;        // ConcentricSpheresIntersector terms
 };
 
+// The background tables of a ray's grid: the launch's (IoP), or in a batch launch those of the
+// ray's grid descriptor (nl == 0: the grid has none).
+struct BgSrc {
+  const int32_t* links;
+  const float* data;
+  float* grad;
+  uint8_t* mask;
+  long long cap;
+  int reso, nl;
+};
+
+__device__ __forceinline__ void load_batch_bg(const svx_batch_grid_t* bgs, int gi, BgSrc& s) {
+  const svx_batch_grid_t& d = bgs[gi];
+  s.nl = d.grid.background_nlayers;
+  s.links = d.grid.background_links;
+  s.data = d.grid.background_data;
+  s.cap = d.grid.background_capacity;
+  s.reso = d.grid.background_reso;
+  s.grad = d.grads.grad_background_out;
+  s.mask = d.grads.mask_background_out;
+}
+
 // ray_find_bounds_bg, render_util.cuh:630-676 (transform_coord, _get_delta_scale, then the
 // sphere frame), _dist_ray_to_origin (cuda_util.cuh:112-119).
 __device__ __forceinline__ void bg_setup(BgArgs& b, const float org[3], const float dir[3], const GridP& g,
-                                         const OptP& opt, const IoP& io) {
-  b.links = io.bg_links;
-  b.data = io.bg_data;
-  b.grad = io.grad_bg;
-  b.mask = io.mask_bg;
-  b.cap = io.bg_cap;
-  b.reso = io.bg_reso;
-  b.nl = io.bg_nl;
-  b.n_steps = (int)__fdiv_rn((float)io.bg_nl, opt.step) + 2;
+                                         const OptP& opt, const BgSrc& src) {
+  b.links = src.links;
+  b.data = src.data;
+  b.grad = src.grad;
+  b.mask = src.mask;
+  b.cap = src.cap;
+  b.reso = src.reso;
+  b.nl = src.nl;
+  b.n_steps = (int)__fdiv_rn((float)src.nl, opt.step) + 2;
   b.brightness = opt.bg;
   b.log_stop = opt.log_stop;
   float o[3], d[3];
@@ -1052,6 +1074,14 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 5 : 4) render_kernel(
     GridP g = g0;
     GridOut go{io.grad_density, io.grad_sh, io.mask, io.accum, io.accum_stride, io.norm, io.beta, io.sparsity};
     if (MULTI) load_batch_grid(io.batch_grids, __ldg(io.ray_grid + ray), g, go);
+    BgSrc bsrc;
+    if constexpr (BG) {
+      if constexpr (MULTI) {
+        load_batch_bg(io.batch_grids, __ldg(io.ray_grid + ray), bsrc);
+      } else {
+        bsrc = BgSrc{io.bg_links, io.bg_data, io.grad_bg, io.mask_bg, io.bg_cap, io.bg_reso, io.bg_nl};
+      }
+    }
     const ShT* __restrict__ sh = reinterpret_cast<const ShT*>(g.sh);
     if (lane == 0) next = atomicAdd(io.work, 1ull);  // prefetch the following ray
     // ---- ray setup (all lanes, redundantly)
@@ -1186,11 +1216,13 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 5 : 4) render_kernel(
     float tb0, tb1, tb2;
     BgArgs bga;
     const float lt_bg = MODE == kBwd ? lt : lt_fwd;
-    const bool with_bg = BG && lt_bg >= -25.f;   // render_background_kernel's cut
+    bool with_bg = false;
     if constexpr (BG) {
-      tb0 = tb1 = tb2 = 0.f;
+      with_bg = bsrc.nl > 0 && lt_bg >= -25.f;   // render_background_kernel's cut
+      // a grid without a background (in a batch launch) keeps the brightness term
+      tb0 = tb1 = tb2 = bsrc.nl > 0 ? 0.f : __fmul_rn(expf(lt_fwd), opt.bg);
       if (with_bg) {
-        bg_setup(bga, org, dir, g, opt, io);
+        bg_setup(bga, org, dir, g, opt, bsrc);
         const float3 c = bg_forward(bga, lt_bg, lane, &bg_evals);
         tb0 = c.x;
         tb1 = c.y;
@@ -1451,6 +1483,9 @@ int dispatch_bd(int bd, int dt, const GridP& g, const OptP& opt, const IoP& io, 
 // Launches the render kernel of a grid with the MSI background (render_bg.cu).
 int dispatch_bg(int mode, bool image, int bd, int dt, const GridP& g, const OptP& opt, const IoP& io,
                 long long n, cudaStream_t st);
+// Launches the batch kernel (SH9) whose grids may have an MSI background (render_bg.cu).
+int dispatch_bg_batch(int mode, int dt, const GridP& g, const OptP& opt, const IoP& io, long long n,
+                      cudaStream_t st);
 
 }  // namespace rk
 }  // namespace svx

@@ -74,6 +74,12 @@ class TrainRequest:
     tv_sh: float = 1e-3
     tv_frac: float = 0.01
     tv_seed: int = 0                  # start of the TV cell windows (host RNG, as the reference)
+    # grids with an MSI background (the reference's opt/opt.py defaults, 113-127 and 226-229)
+    lr_sigma_bg: float = 3.0
+    lr_color_bg: float = 0.1
+    tv_background_sigma: float = 1e-2
+    tv_background_color: float = 1e-2
+    tv_background_frac: float = 0.01
 
 
 @dataclass
@@ -260,6 +266,10 @@ def grid_bytes(grid, trainable: bool) -> int:
         N, Cc = grid.sh_data.shape
         n += 2 * (N * 4 + N * Cc * 4) + N          # gradients, RMSprop state, mask
         n += N * ((Cc + 1 + 3) // 4 * 4) * 4       # padded accumulation rows
+    if grid.use_background:
+        n += grid.background_links.numel() * 4 + grid.background_data.numel() * 4
+        if trainable:
+            n += 2 * grid.background_data.numel() * 4 + grid.background_data[..., 0].numel()
     return int(n)
 
 
@@ -304,6 +314,7 @@ class RenderServer:
                          if isinstance(t, torch.Tensor))
         self.sched.budget -= lane_bytes
         self.slots_free = list(range(max_grids))
+        self.with_bg = False             # some resident grid has an MSI background
         self.batches = {"render": 0, "train": 0}
         self.accum_min_rays = 1 << 15  # train steps this large accumulate into padded rows (vector atomics)
         self.lane_depth = 2          # batches a lane may have queued on the device
@@ -334,12 +345,26 @@ class RenderServer:
             g["mask"] = torch.zeros((N,), dtype=torch.bool, device=self.device)
             g["accum"] = torch.zeros((N, (Cc + 1 + 3) // 4 * 4), dtype=torch.float32, device=self.device)
             grid._get_data_grads()
+            if grid.use_background:
+                g["mask_bg"] = torch.zeros(grid.background_data.shape[:2], dtype=torch.bool, device=self.device)
+                grid._grad_buffer(grid.background_data)
         self.grids[grid_id] = g
         self._set_desc(grid_id, 0.0)
+        self._update_background_flag()
 
     def remove_grid(self, grid_id: str) -> None:
         self.sched.remove_grid(grid_id)
         self.slots_free.append(self.grids.pop(grid_id)["slot"])
+        self._update_background_flag()
+
+    def _update_background_flag(self) -> None:
+        """Batches run the background kernel while some resident grid has an MSI background;
+        the lanes' captured graphs are dropped when that changes."""
+        flag = any(g["grid"].use_background for g in self.grids.values())
+        if flag != self.with_bg:
+            for lane in self.lanes.values():
+                lane["graph"] = None
+        self.with_bg = flag
 
     def _set_desc(self, grid_id: str, norm: float, use_accum: bool = False) -> None:
         _lib = self._lib
@@ -349,6 +374,9 @@ class RenderServer:
         if g["trainable"]:
             gd, gs = g["grid"]._get_data_grads()
             d.grads = _lib.SvxGridGrads(gd.data_ptr(), gs.data_ptr(), g["mask"].data_ptr())
+            if "mask_bg" in g:
+                d.grads.grad_background_out = g["grid"]._grad_buffer(g["grid"].background_data).data_ptr()
+                d.grads.mask_background_out = g["mask_bg"].data_ptr()
             if use_accum:
                 d.accum = g["accum"].data_ptr()
                 d.accum_stride = g["accum"].size(1)
@@ -426,7 +454,8 @@ class RenderServer:
         order = lane["order"].data_ptr() if name == "train" else None
 
         def call():
-            _lib.call("svx_render_batch", mode, lane["desc"].data_ptr(), 9, dt, lane["origins"].data_ptr(),
+            _lib.call("svx_render_batch", mode, lane["desc"].data_ptr(), 9, dt, int(self.with_bg),
+                      lane["origins"].data_ptr(),
                       lane["dirs"].data_ptr(), lane["ray_grid"].data_ptr(), order, lane["n_rays"].data_ptr(),
                       self.sched.batch_rays, C.byref(self.opt), lane["rgb_gt"].data_ptr(),
                       lane["rgb_out"].data_ptr(), lane["work"].data_ptr(), torch.cuda.current_stream().cuda_stream)
@@ -527,6 +556,8 @@ class RenderServer:
                 _lib.call("svx_ray_order", C.byref(g["struct"]), C.byref(rays), C.byref(self.opt),
                           off, lane["order"][sl].data_ptr(), st.cuda_stream)
                 g["mask"].zero_()
+                if "mask_bg" in g:
+                    g["mask_bg"].zero_()
                 use_accum = t.n_rays >= self.accum_min_rays
                 if use_accum:
                     g["accum"].zero_()
@@ -553,8 +584,18 @@ class RenderServer:
                 grid.inplace_tv_grad(grid._grad_buffer(grid.density_data), scaling=r.tv_density,
                                      sparse_frac=r.tv_frac)
                 grid.inplace_tv_color_grad(grid._grad_buffer(grid.sh_data), scaling=r.tv_sh, sparse_frac=r.tv_frac)
+                if "mask_bg" in g:
+                    grid.sparse_background_indexer = g["mask_bg"]
+                    if r.tv_background_sigma > 0.0 or r.tv_background_color > 0.0:
+                        grid.inplace_tv_background_grad(grid._grad_buffer(grid.background_data),
+                                                        scaling=r.tv_background_color,
+                                                        scaling_density=r.tv_background_sigma,
+                                                        sparse_frac=r.tv_background_frac, contiguous=True)
                 grid.optim_density_step(r.lr_density, beta=r.rms_beta)
                 grid.optim_sh_step(r.lr_sh, beta=r.rms_beta)
+                if "mask_bg" in g:
+                    grid.optim_background_step(r.lr_sigma_bg, r.lr_color_bg, beta=r.rms_beta)
+                    grid.sparse_background_indexer = None
                 grid.sparse_grad_indexer = None
                 grid.sparse_sh_grad_indexer = None
             ev = torch.cuda.Event()

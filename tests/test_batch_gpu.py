@@ -40,7 +40,7 @@ def _order(spec, o, d, opt, base, out):
               base, out.data_ptr(), torch.cuda.current_stream().cuda_stream)
 
 
-def _batch(mode, grids, rays, opt, sh_dtype, use_order, accum_for=()):
+def _batch(mode, grids, rays, opt, sh_dtype, use_order, accum_for=(), with_bg=0):
     """One svx_render_batch launch over every grid's rays; returns rgb per grid and the
     per-grid gradient buffers (accumulation rows already flushed)."""
     dev = "cuda"
@@ -61,6 +61,11 @@ def _batch(mode, grids, rays, opt, sh_dtype, use_order, accum_for=()):
         desc.grid = csrc._grid_struct(spec)
         if mode == 1:
             desc.grads = _lib.SvxGridGrads(b["gd"].data_ptr(), b["gs"].data_ptr(), b["mask"].data_ptr())
+            if spec.background_data is not None:
+                b["gbg"] = torch.zeros(spec.background_data.shape, device=dev)
+                b["mbg"] = torch.zeros(spec.background_data.shape[:2], dtype=torch.bool, device=dev)
+                desc.grads.grad_background_out = b["gbg"].data_ptr()
+                desc.grads.mask_background_out = b["mbg"].data_ptr()
             desc.norm = 2.0 / (3 * o.shape[0])
             if i in accum_for:
                 b["accum"] = torch.zeros((N, (Cc + 1 + 3) // 4 * 4), device=dev)
@@ -77,7 +82,8 @@ def _batch(mode, grids, rays, opt, sh_dtype, use_order, accum_for=()):
     rgb = torch.zeros((n, 3), device=dev)
     dt = {torch.float32: _lib.SVX_F32, torch.bfloat16: _lib.SVX_BF16, torch.float16: _lib.SVX_F16}[sh_dtype]
     st = torch.cuda.current_stream().cuda_stream
-    _lib.call("svx_render_batch", mode, table.data_ptr(), 9, dt, O_.data_ptr(), D_.data_ptr(), ray_grid.data_ptr(),
+    _lib.call("svx_render_batch", mode, table.data_ptr(), 9, dt, with_bg, O_.data_ptr(), D_.data_ptr(),
+              ray_grid.data_ptr(),
               order.data_ptr() if use_order else None, n_dev.data_ptr(), n, C.byref(csrc._opt_struct(opt)),
               GT.data_ptr() if mode == 1 else None, rgb.data_ptr(), work.data_ptr(), st)
     for (spec, _), b in zip(grids, bufs):
@@ -173,3 +179,63 @@ def test_add_accum_adds_nonzero_rows_only():
     assert torch.equal(torch.signbit(S_.cpu()[::3, 0]), torch.ones(N // 3, dtype=torch.bool))
     with pytest.raises(RuntimeError, match="stride"):
         _lib.call("svx_add_accum", A.data_ptr(), 26, Cc, N, S_.data_ptr(), D.data_ptr(), None)
+
+
+def _with_background(grids, rays, which, seed=40):
+    """Give the grids listed in `which` an MSI background of their own, and send half of their
+    rays off in random directions."""
+    for i in which:
+        spec, og = grids[i]
+        gen = torch.Generator().manual_seed(seed + i)
+        reso, nl = 8 + 2 * i, 4 + i
+        keep = torch.rand((2 * reso, reso), generator=gen) >= 0.2
+        bl = torch.full(keep.shape, -1, dtype=torch.int32)
+        bl[keep] = torch.arange(int(keep.sum()), dtype=torch.int32)
+        bd = torch.randn((int(keep.sum()), nl, 4), generator=gen) * 0.5
+        bd[..., 3] = torch.rand((int(keep.sum()), nl), generator=gen) * 4.0 - 0.5
+        spec.background_links, spec.background_data = bl.cuda(), bd.cuda()
+        og.bg_links, og.bg_data = bl.numpy(), bd.numpy()
+        o, d, gt = rays[i]
+        q = o.shape[0]
+        dr = torch.randn((q // 2, 3), generator=gen)
+        d = d.clone()
+        d[q // 2:] = dr / dr.norm(dim=-1, keepdim=True)
+        rays[i] = (o, d.contiguous(), gt)
+
+
+@pytest.mark.parametrize("use_order", [False, True])
+def test_batch_with_background_matches_oracle_per_grid(use_order):
+    """Grids 0 and 2 carry MSI backgrounds, grid 1 none: one launch renders and differentiates
+    each ray against its own grid's background (or brightness)."""
+    opt, oopt = opt_struct(stop_thresh=0.0)
+    grids, rays = _setup(torch.float32, seed=31)
+    _with_background(grids, rays, (0, 2))
+    rgbs, bufs = _batch(1, grids, rays, opt, torch.float32, use_order, accum_for=(1,), with_bg=1)
+    for i, ((spec, og), (o, d, gt), rgb, b) in enumerate(zip(grids, rays, rgbs, bufs)):
+        ref = O.render(og, oopt, o.numpy(), d.numpy(), mode=1, rgb_gt=gt.numpy(), prec="f64")
+        err = np.abs(rgb - ref["rgb"]).max()
+        assert err <= 5e-5, (i, err)
+        for k, key in (("gd", "grad_density"), ("gs", "grad_sh"), ("gbg", "grad_background")):
+            if k not in b:
+                continue
+            r = ref[key]
+            bad = np.abs(b[k].cpu().numpy() - r) > 1e-3 * np.abs(r) + 1e-4 * max(np.abs(r).max(), 1e-30)
+            assert not bad.any(), (i, key, int(bad.sum()))
+        if "mbg" in b:
+            assert np.abs(ref["grad_background"]).max() > 0
+            # a sample on a cell boundary may fall in either cell (the kernel's norms round
+            # differently from the float64 oracle's): a few rows of zero weight may differ
+            diff = int((b["mbg"].cpu().numpy() != ref["mask_background"]).sum())
+            assert diff <= max(4, ref["mask_background"].size // 200), (i, diff)
+
+
+def test_batch_render_with_background_equals_single_grid():
+    """Forward colours of the batch launch equal the single-grid render of each grid, with
+    and without its background."""
+    opt, _ = opt_struct()
+    grids, rays = _setup(torch.float32, seed=37)
+    _with_background(grids, rays, (1,))
+    batch, _ = _batch(0, grids, rays, opt, torch.float32, True, with_bg=1)
+    for (spec, og), (o, d, _), a in zip(grids, rays, batch):
+        alone = csrc.volume_render_cuvol(spec, _rays(o, d), opt).cpu().numpy()
+        np.testing.assert_array_equal(a, alone)

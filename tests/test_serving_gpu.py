@@ -93,3 +93,74 @@ def test_admission_rejects_over_budget_grid():
         server.add_grid("big", _grid(g), trainable=True)
     with pytest.raises(ValueError):
         server.submit(RenderRequest("missing", torch.eye(4), 8, 8, fx=10.0))
+
+
+def _bg_grid(g, seed):
+    grid = _grid(g)
+    gen = torch.Generator().manual_seed(seed)
+    reso, nl = 12, 6
+    grid.background_nlayers, grid.background_reso = nl, reso
+    grid.background_links = torch.arange(2 * reso * reso, dtype=torch.int32, device="cuda").view(2 * reso, reso)
+    bd = torch.randn((2 * reso * reso, nl, 4), generator=gen) * 0.5
+    bd[..., 3] = torch.rand((2 * reso * reso, nl), generator=gen) * 2.0
+    grid.background_data = torch.nn.Parameter(bd.cuda())
+    return grid
+
+
+def test_serving_with_background_matches_serial_replay():
+    """A resident grid with an MSI background next to one without: the batch launches render
+    and train both, and every result equals the plain API's (background TV and optimiser step
+    included in the train step)."""
+    spec = {"b0": (32, 0.3), "g1": (24, 0.4)}
+    data = {k: S.make_grid(r, occupancy=o, seed=90 + i) for i, (k, (r, o)) in enumerate(spec.items())}
+    trainable = {"b0", "g1"}
+
+    def make(k):
+        return _bg_grid(data[k], 7) if k == "b0" else _grid(data[k])
+
+    server = RenderServer(hbm_budget=8e9, batch_rays=16384, chunk_rays=2048, use_graphs=True)
+    live = {k: make(k) for k in spec}
+    for k, grid in live.items():
+        server.add_grid(k, grid, trainable=k in trainable)
+    assert server.with_bg
+    reqs = _requests(24, list(spec), trainable, seed=9)
+    tickets = [server.submit(r) for r in reqs]
+    server.run_until_idle()
+    assert all(t.state == "done" for t in tickets)
+
+    ref = {k: make(k) for k in spec}
+    touched = set()
+    for r, t in zip(reqs, tickets):
+        grid = ref[r.grid_id]
+        if isinstance(r, RenderRequest):
+            with torch.no_grad():
+                img = grid.volume_render_image(Camera(r.c2w.cuda(), fx=r.fx, width=r.width, height=r.height)).cpu()
+            if r.grid_id in touched:
+                assert float((img - t.result).abs().max()) <= 1e-3
+            else:
+                assert torch.equal(img, t.result), "render differs from the same render alone"
+        else:
+            rgb = grid.volume_render_fused(Rays(r.origins.cuda(), r.dirs.cuda()), r.rgb_gt.cuda())
+            np.random.seed(r.tv_seed)
+            grid.inplace_tv_grad(grid._grad_buffer(grid.density_data), scaling=r.tv_density, sparse_frac=r.tv_frac)
+            grid.inplace_tv_color_grad(grid._grad_buffer(grid.sh_data), scaling=r.tv_sh, sparse_frac=r.tv_frac)
+            if grid.use_background:
+                grid.inplace_tv_background_grad(grid._grad_buffer(grid.background_data),
+                                                scaling=r.tv_background_color, scaling_density=r.tv_background_sigma,
+                                                sparse_frac=r.tv_background_frac, contiguous=True)
+            grid.optim_density_step(r.lr_density, beta=r.rms_beta)
+            grid.optim_sh_step(r.lr_sh, beta=r.rms_beta)
+            if grid.use_background:
+                grid.optim_background_step(r.lr_sigma_bg, r.lr_color_bg, beta=r.rms_beta)
+            rgb = rgb.cpu()
+            if r.grid_id in touched:
+                assert float((rgb - t.result).abs().max()) <= 1e-3
+            else:
+                assert torch.equal(rgb, t.result)
+            touched.add(r.grid_id)
+    assert "b0" in touched
+    d = float((ref["b0"].background_data.detach() - live["b0"].background_data.detach()).abs().max())
+    assert d <= 1e-3, d
+    assert float((ref["b0"].background_data.detach() - _bg_grid(data["b0"], 7).background_data.detach()).abs().max()) > 0
+    server.remove_grid("b0")
+    assert not server.with_bg

@@ -936,22 +936,30 @@ __device__ __forceinline__ void bg_chunk(const BgArgs& b, int i0, int lane, floa
   c.width = __fsub_rn(invr_last, invr);
   c.pcnt = __fmul_rn(__fmul_rn(c.width, b.ws), c.v[3]);
   unsigned em = __ballot_sync(kFull, c.valid && c.v[3] > 0.f);
-  c.lt_before = 0.f;
-  c.lt_after = 0.f;
-  c.stopped = false;
-  unsigned m = em;
-  while (m) {
-    const int k = __ffs(m) - 1;
-    m &= m - 1;
-    const float pc = __shfl_sync(kFull, c.pcnt, k);
-    if (lane == k) c.lt_before = lt;
-    lt = __fsub_rn(lt, pc);
-    if (lane == k) c.lt_after = lt;
-    if (lt < b.log_stop) {
-      em &= (k == 31) ? kFull : ((2u << k) - 1u);
-      c.stopped = true;
-      break;
-    }
+  // Optical depth before and after each counted sample, as a prefix sum over the chunk.  The
+  // reference subtracts the samples one by one; the sums differ from that sequence in the last
+  // bits only.  The early stop cuts the chunk after the first counted sample whose
+  // transmittance falls below the threshold, as the reference's break does.
+  const bool mine = (em >> lane) & 1u;
+  const float x = mine ? c.pcnt : 0.f;
+  float incl = x;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const float y = __shfl_up_sync(kFull, incl, d);
+    if (lane >= d) incl = __fadd_rn(incl, y);
+  }
+  float excl = __shfl_up_sync(kFull, incl, 1);
+  if (lane == 0) excl = 0.f;
+  c.lt_before = __fsub_rn(lt, excl);
+  c.lt_after = __fsub_rn(lt, incl);
+  const unsigned under = __ballot_sync(kFull, mine && c.lt_after < b.log_stop);
+  c.stopped = under != 0u;
+  if (c.stopped) {
+    const int k = __ffs(under) - 1;
+    em &= (k == 31) ? kFull : ((2u << k) - 1u);
+    lt = __shfl_sync(kFull, c.lt_after, k);
+  } else {
+    lt = __shfl_sync(kFull, c.lt_after, 31);
   }
   c.em = em;
 }

@@ -209,3 +209,56 @@ def test_sparsify_background_matches_reference_without_dilation():
     np.testing.assert_array_equal(g.background_data.data.numpy(), z["data_out"])
     with pytest.raises(RuntimeError):
         g.sparsify_background(dilate=1)   # the dilation is a CUDA kernel
+
+
+def test_oracle_msi_tv_known_answer():
+    """msi_tv_grad_sparse (loss_kernel.cu:248-333) on a 2 x 1 x 2 MSI, worked out by hand:
+    x wraps (the neighbour of column 1 is column 0), y has one row (its neighbour is itself,
+    dy = 0), z stops at the last layer, where a colour channel compares with itself and sigma
+    with 0.  Scales are divided by the cell count."""
+    links = np.array([[0], [1]], np.int32)                    # [2 reso, reso], reso = 1
+    msi = np.array([[[1.0, 2.0], [3.0, 5.0]],                 # cell (0,0): layers 0, 1; (colour, sigma)
+                    [[4.0, 1.0], [0.0, 2.0]]], np.float32)    # cell (1,0)
+    cells = np.array([0, 1, 2, 3], np.int32)                   # (x, y, z) = (0,0,0) (0,0,1) (1,0,0) (1,0,1)
+    s, s_last = 0.8, 0.4
+    g = O.msi_tv_grad(links, msi, cells, s, s_last, prec="f64")
+    exp = np.zeros_like(msi, dtype=np.float64)
+    sx, sy, sz = 2 / 256, 1 / 256, 2 / 256
+
+    m64 = msi.astype(np.float64)
+    s, s_last = float(np.float32(s)), float(np.float32(s_last))   # the float32 scales the call passes
+
+    def term(x, z, ch):
+        nl = 2
+        v00 = m64[x, z, ch]
+        vz = m64[x, z + 1, ch] if z + 1 < nl else (0.0 if ch == 1 else v00)
+        v10 = m64[1 - x, z, ch]
+        dx, dy, dz = v10 - v00, 0.0, vz - v00
+        scale = float(np.float32(s_last) / np.float32(4)) if ch == 1 else float(np.float32(s) / np.float32(4))
+        idelta = scale / np.sqrt(float(np.float32(1e-9)) + dx * dx + dy * dy + dz * dz)
+        dx, dz = dx * sx, dz * sz
+        exp[x, z, ch] += -(dx + dz) * idelta
+        if z + 1 < nl:
+            exp[x, z + 1, ch] += dz * idelta
+        exp[1 - x, z, ch] += dx * idelta
+
+    for x in range(2):
+        for z in range(2):
+            for ch in range(2):
+                term(x, z, ch)
+    np.testing.assert_allclose(g, exp, rtol=1e-12, atol=1e-15)
+
+
+def test_rand_cells_background_window_wraps():
+    """_get_rand_cells_background: max(int(frac * n), 1) contiguous cells over the
+    [2 reso, reso, nlayers] cells from a host RNG start, wrapping at the end."""
+    g = SparseGrid(reso=4, basis_dim=1, background_nlayers=3, background_reso=4)
+    n = 2 * 4 * 4 * 3
+    for seed in range(20):
+        np.random.seed(seed)
+        cells = g._get_rand_cells_background(0.25, contiguous=True).numpy()
+        assert cells.shape == (int(0.25 * n),)
+        assert cells.min() >= 0 and cells.max() < n
+        assert np.all((np.diff(cells) == 1) | (np.diff(cells) == 1 - n))
+    np.random.seed(0)
+    assert g._get_rand_cells_background(0.0).shape == (1,)

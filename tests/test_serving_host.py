@@ -170,3 +170,16 @@ def test_train_step_waits_for_device_work_not_host_readback():
     done.add(r.id)                            # the render's kernels finished; its colours are still
     _, trains = s.plan()                      # on their way to the host
     assert trains == [tr]
+
+
+def test_grid_bytes_count_the_background_tables():
+    """Admission charges a grid's MSI background: its tables, and when trainable its gradient,
+    RMSprop state and mask."""
+    from svox2_gb300 import SparseGrid
+    from svox2_gb300.serving import grid_bytes
+    plain = SparseGrid(reso=8, basis_dim=9)
+    bg = SparseGrid(reso=8, basis_dim=9, background_nlayers=3, background_reso=4)
+    tables = 2 * 4 * 4 * 4 + 2 * 4 * 4 * 3 * 4 * 4          # links + data [32, 3, 4] float32
+    assert grid_bytes(bg, False) - grid_bytes(plain, False) == tables
+    train_extra = 2 * (2 * 4 * 4 * 3 * 4 * 4) + 2 * 4 * 4 * 3  # gradient + RMSprop state + mask
+    assert grid_bytes(bg, True) - grid_bytes(plain, True) == tables + train_extra

@@ -1,4 +1,6 @@
-// Ray march, fused MSE adjoint and image render for the `cuvol` backend.
+// Ray march, fused MSE adjoint and image render for the `cuvol` backend: host side,
+// and the instantiations for grids without the MSI background (render_bg.cu holds those
+// with it).  The kernel template itself is in render_core.cuh.
 //
 // Replaces svox2/csrc/render_lerp_kernel_cuvol.cu (trace_ray_cuvol 30-120,
 // trace_ray_cuvol_backward 227-383, kernels 611-773, host 918-1152) with one
@@ -6,31 +8,8 @@
 //   kFwd   volume_render_cuvol / volume_render_cuvol_image
 //   kFused volume_render_cuvol_fused   (forward, MSE residual, adjoint)
 //   kBwd   volume_render_cuvol_backward (forward, given dL/drgb, adjoint)
-//
-// Work decomposition (one warp per ray, persistent warps pulling rays from a
-// counter):
-//   * Prologue, lanes = samples.  32 consecutive samples of the ray at once:
-//     each lane forms its sample's t (sequential float adds, as the reference
-//     does), grid position, cell, the 8 corner links and the trilinear density.
-//     Transmittance is then carried through the evaluated lanes in order with
-//     one subtraction per sample, exactly the reference's sequence.
-//   * Colour, lanes = (colour channel g, cell corner j), 3 x 8 = 24 lanes.
-//     Because the SH basis is fixed for the ray, each corner's colour is
-//     reduced to D[j][g] = sum_k basis_k * sh[link_j][g*bd + k] once per cell
-//     the ray enters, and a sample's colour is sum_j w_j(pos) D[j][g] — three
-//     numbers per corner instead of 27.  Corners shared with the previous cell
-//     move between lanes by shuffle; only new corners are gathered, with the
-//     27 coefficients of a voxel read by 27 consecutive lanes.
-//   * Adjoint, reverse order.  The forward pass stores a checkpoint (t, log T,
-//     sample index) per 32-sample segment that holds evaluated samples, and the
-//     per-sample colours (up to the cache capacity).  The adjoint walks the
-//     segments last to first, recomputes each segment's samples and
-//     transmittance from its checkpoint, and accumulates the light-after-sample
-//     term as a suffix sum, so no colour_cache dot product is subtracted down to
-//     the cancellation floor.  The gradient of d(colour)/d(sh) factorises as
-//     basis_k * B[j][g]; B is summed in registers over all samples that share a
-//     corner and flushed with one coalesced 27-wide atomic add per corner when
-//     the ray leaves it (the reference issues 8 x 27 atomics per sample).
+// plus the depth renders (depth_kernel), grid_weight_render (grid_weight_kernel), the
+// coherence ray order and the accumulation-row flush.
 
 #include "render_core.cuh"
 

@@ -2,6 +2,31 @@
 // runs and colours, the gradient flushes, and the render kernel template with its launcher.
 // Shared by render.cu (grids without a background) and render_bg.cu (grids with the MSI
 // background model), which compile their instantiations in parallel.
+//
+// Work decomposition (one warp per ray, persistent warps pulling rays from a
+// counter):
+//   * Prologue, lanes = samples.  32 consecutive samples of the ray at once:
+//     each lane forms its sample's t (sequential float adds, as the reference
+//     does), grid position, cell, the 8 corner links and the trilinear density.
+//     Transmittance is then carried through the evaluated lanes in order with
+//     one subtraction per sample, exactly the reference's sequence.
+//   * Colour, lanes = (colour channel g, cell corner j), 3 x 8 = 24 lanes.
+//     Because the SH basis is fixed for the ray, each corner's colour is
+//     reduced to D[j][g] = sum_k basis_k * sh[link_j][g*bd + k] once per cell
+//     the ray enters, and a sample's colour is sum_j w_j(pos) D[j][g] — three
+//     numbers per corner instead of 27.  Corners shared with the previous cell
+//     move between lanes by shuffle; only new corners are gathered, with the
+//     27 coefficients of a voxel read by 27 consecutive lanes.
+//   * Adjoint, reverse order.  The forward pass stores a checkpoint (t, log T,
+//     sample index) per 32-sample segment that holds evaluated samples, and the
+//     per-sample colours (up to the cache capacity).  The adjoint walks the
+//     segments last to first, recomputes each segment's samples and
+//     transmittance from its checkpoint, and accumulates the light-after-sample
+//     term as a suffix sum, so no colour_cache dot product is subtracted down to
+//     the cancellation floor.  The gradient of d(colour)/d(sh) factorises as
+//     basis_k * B[j][g]; B is summed in registers over all samples that share a
+//     corner and flushed with one coalesced 27-wide atomic add per corner when
+//     the ray leaves it (the reference issues 8 x 27 atomics per sample).
 #pragma once
 #include "common.cuh"
 

@@ -24,7 +24,7 @@ from torch import autograd, nn
 
 from . import csrc as _C
 from . import utils
-from .defs import BASIS_TYPE_SH
+from .defs import BASIS_TYPE_3D_TEXTURE, BASIS_TYPE_MLP, BASIS_TYPE_SH
 
 
 def _no_cpu_path(what: str):
@@ -411,6 +411,15 @@ class SparseGrid(nn.Module):
     @property
     def shape(self):
         return list(self.links.shape) + [self.data_dim]
+
+    def basis_type_name(self):
+        """Name of the basis type (svox2/svox2.py:2110-2117)."""
+        return {BASIS_TYPE_SH: "SH", BASIS_TYPE_3D_TEXTURE: "3D_TEXTURE", BASIS_TYPE_MLP: "MLP"}.get(
+            self.basis_type, "UNKNOWN")
+
+    def __repr__(self):
+        return (f"svox2.SparseGrid(basis_type={self.basis_type_name()}, basis_dim={self.basis_dim}, "
+                f"reso={list(self.links.shape)}, capacity:{self.sh_data.size(0)})")
 
     def is_cubic_pow2(self):
         r = self.links.shape
@@ -952,5 +961,5 @@ class SparseGrid(nn.Module):
         raise NotImplementedError("this SparseGrid method is not implemented in svox2_gb300")
 
     resize = to_svox1 = _unbuilt
-    inplace_tv_lumisphere_grad = inplace_tv_basis_grad = _unbuilt
-    optim_basis_step = _unbuilt
+    inplace_tv_lumisphere_grad = inplace_tv_basis_grad = tv_basis = _unbuilt
+    optim_basis_step = reinit_learned_bases = _unbuilt

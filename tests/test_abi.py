@@ -113,3 +113,27 @@ def test_background_grids_are_validated_on_the_host():
     rc = lib.svx_msi_tv_grad_sparse(0x1000, 0, 0x2000, 32, 3, 4, 0x3000, 8, None, C.c_float(1.0), C.c_float(1.0),
                                     0x4000, None)
     assert rc == _lib.SVX_ERR_INVALID and b"reso" in lib.svx_last_error()
+
+
+def test_sparse_grid_has_the_reference_method_surface():
+    """Every public SparseGrid method of the reference (svox2/svox2.py:335-2357) exists here; the
+    ones outside this library's scope (learned/MLP bases, lumisphere TV, resize, svox1 export)
+    raise NotImplementedError when called."""
+    from svox2_gb300 import SparseGrid
+    public = ["accelerate", "basis_type_name", "forward", "grid2world", "inplace_l2_color_grad",
+              "inplace_tv_background_grad", "inplace_tv_basis_grad", "inplace_tv_color_grad", "inplace_tv_grad",
+              "inplace_tv_lumisphere_grad", "is_cubic_pow2", "load", "optim_background_step", "optim_basis_step",
+              "optim_density_step", "optim_sh_step", "reinit_learned_bases", "resample", "resize", "sample", "save",
+              "sparsify_background", "to_svox1", "tv", "tv_basis", "tv_color", "volume_render",
+              "volume_render_depth", "volume_render_depth_image", "volume_render_fused", "volume_render_image",
+              "world2grid", "data_dim", "basis_reso", "use_background", "shape"]
+    missing = [m for m in public if not hasattr(SparseGrid, m)]
+    assert not missing, missing
+    g = SparseGrid(reso=4, basis_dim=1)
+    for m in ("resize", "to_svox1", "tv_basis", "reinit_learned_bases", "optim_basis_step",
+              "inplace_tv_lumisphere_grad", "inplace_tv_basis_grad"):
+        try:
+            getattr(g, m)()
+        except NotImplementedError:
+            continue
+        raise AssertionError(f"{m} should raise NotImplementedError")

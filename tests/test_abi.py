@@ -137,3 +137,20 @@ def test_sparse_grid_has_the_reference_method_surface():
         except NotImplementedError:
             continue
         raise AssertionError(f"{m} should raise NotImplementedError")
+
+
+def test_operator_module_has_the_reference_op_table():
+    """svox2_gb300.csrc exports every operator the reference registers (svox2/csrc/svox2.cpp:74-112)
+    for the cuvol backend, the TV/MSI losses, the optimisers and the grid utilities.  Left out,
+    and absent so that name lookups fail as with a module that lacks them: the nvol and svox1
+    backends and lumisphere TV."""
+    import svox2_gb300.csrc as C
+    ops = ["volume_render_cuvol", "volume_render_cuvol_image", "volume_render_cuvol_backward",
+           "volume_render_cuvol_fused", "volume_render_expected_term", "volume_render_sigma_thresh",
+           "sample_grid", "sample_grid_backward", "dilate", "accel_dist_prop", "grid_weight_render", "tv",
+           "tv_grad", "tv_grad_sparse", "msi_tv_grad_sparse", "rmsprop_step", "sgd_step"]
+    assert [n for n in ops if not hasattr(C, n)] == []
+    for n in ("volume_render_nvol", "volume_render_svox1_fused", "lumisphere_tv_grad_sparse"):
+        assert not hasattr(C, n)
+    for cls in ("SparseGridSpec", "CameraSpec", "RaysSpec", "RenderOptions", "GridOutputGrads"):
+        assert hasattr(C, cls)

@@ -205,11 +205,12 @@ int svx_volume_render_sigma_thresh(const svx_grid_t* grid, const svx_rays_t* ray
  * svx_volume_render_cuvol_fused; it calls no cudaMalloc/cudaFree and no
  * allocating routine.  Its scratch (the ray counter) is a 256-byte static
  * device array held by every GPU that loads the library until exit; a call
- * needs 8 bytes of it, and a larger need is rejected with SVX_ERR_TOO_LARGE.
- * The first call on a device looks the array's address up (once per device)
- * and should come before any stream capture on that device.  All calls
- * share the array: calls that overlap on the GPU race on the counter and
- * must be serialised by the caller. */
+ * needs 8 bytes of it whatever the number of rays or the grid's size, which
+ * the library checks against the array when it is compiled.  The first call
+ * on a device looks the array's address up (again after a device reset) and
+ * should come before any stream capture on that device.  All calls share the
+ * array: calls that overlap on the GPU race on the counter and must be
+ * serialised by the caller. */
 int svx_volume_render_cuvol_fused_noalloc(const svx_grid_t* grid, const svx_rays_t* rays,
                                           const svx_render_opts_t* opt, const float* rgb_gt,
                                           float beta_loss, float sparsity_loss, float* rgb_out,

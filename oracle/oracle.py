@@ -113,10 +113,17 @@ def default_threads() -> int:
 
 def render(grid: Grid, opt: Opt, origins, dirs, mode: int = 0, rgb_gt=None, grad_out=None, color=None,
            beta_loss: float = 0.0, sparsity_loss: float = 0.0, prec: str = "f32", want_grads: bool = True,
-           want_mask: bool = True, trace: bool = False, nthreads: Optional[int] = None) -> dict:
+           want_mask: bool = True, trace: bool = False, nthreads: Optional[int] = None,
+           stops=None, want_magnitude: bool = False) -> dict:
     """volume_render_cuvol (mode 0), _fused (1), _backward (2, color = forward colour).
     With an MSI background the result also holds grad_background [capacity, nlayers, 4] and,
-    in mode 1, mask_background [capacity, nlayers]."""
+    in mode 1, mask_background [capacity, nlayers].
+
+    The result's "stops" holds each ray's early-stop count (-1: no early stop).  Passing a
+    float run's "stops" back in (stops=...) makes every ray stop where that run stopped, so that
+    a "f64" run evaluates exactly the float run's samples (the sampling geometry is float in
+    both precisions).  want_magnitude adds "mag_density" / "mag_sh": per gradient entry, the
+    sum of the absolute values of the terms that make it up (the scale of float rounding)."""
     R = _real(prec)
     origins = np.ascontiguousarray(origins, dtype=np.float32)
     dirs = np.ascontiguousarray(dirs, dtype=np.float32)
@@ -135,6 +142,12 @@ def render(grid: Grid, opt: Opt, origins, dirs, mode: int = 0, rgb_gt=None, grad
     mbg = np.zeros(grid.bg_data.shape[:2], dtype=np.uint8) if (has_bg and mode == 1 and want_mask) else None
     gt = None if rgb_gt is None else np.ascontiguousarray(rgb_gt, dtype=np.float32)
     go = None if grad_out is None else np.ascontiguousarray(grad_out, dtype=np.float32)
+    st_out = np.full((Q,), -1, dtype=np.int32) if mode in (0, 1) else None
+    st_in = None if stops is None else np.ascontiguousarray(stops, dtype=np.int32)
+    if st_in is not None and st_in.shape != (Q,):
+        raise ValueError("stops must hold one entry per ray")
+    md = np.zeros((N, 1), dtype=R) if (mode and want_magnitude) else None
+    ms = np.zeros((N, Cc), dtype=R) if (mode and want_magnitude) else None
     g = grid.struct()
     o = opt.struct()
     fn = getattr(lib(), "oracle_render_" + prec)
@@ -143,10 +156,12 @@ def render(grid: Grid, opt: Opt, origins, dirs, mode: int = 0, rgb_gt=None, grad
        C.c_void_p(_p(gt)), C.c_void_p(_p(go)), C.c_float(beta_loss), C.c_float(sparsity_loss),
        C.c_void_p(_p(rgb)), C.c_void_p(_p(gd)), C.c_void_p(_p(gs)), C.c_void_p(_p(mask)), C.c_void_p(_p(gbg)),
        C.c_void_p(_p(mbg)), C.c_void_p(_p(tr)), C.c_void_p(_p(ne)), C.c_void_p(_p(nb)),
-       C.c_int(nthreads or default_threads()))
+       C.c_int(nthreads or default_threads()), C.c_void_p(_p(st_out)), C.c_void_p(_p(st_in)),
+       C.c_void_p(_p(md)), C.c_void_p(_p(ms)))
     return {"rgb": rgb, "grad_density": gd, "grad_sh": gs, "mask": None if mask is None else mask.astype(bool),
             "grad_background": gbg, "mask_background": None if mbg is None else mbg.astype(bool),
-            "trace": tr, "n_eval": int(ne[0]), "n_background": int(nb[0])}
+            "trace": tr, "n_eval": int(ne[0]), "n_background": int(nb[0]), "stops": st_out,
+            "mag_density": md, "mag_sh": ms}
 
 
 def render_image(grid: Grid, opt: Opt, c2w, fx, fy, cx, cy, width, height, ndc=(-1.0, -1.0), prec="f32",

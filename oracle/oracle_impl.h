@@ -14,6 +14,17 @@
  * for every error statement.  Each function names the reference code it
  * restates (paths inside the reference project).
  *
+ * Sampling geometry is float in both instances: the ray's grid-space origin,
+ * direction and world step, its bounds, every sample's t, cell and position
+ * in the cell, and the skip distances.  Those decide WHICH samples are taken
+ * (links-level parity is bit-exact by requirement), so the double instance
+ * takes exactly the float instance's samples and evaluates every value along
+ * them (densities, colours, weights, transmittance, gradients) in double.
+ * Its per-entry errors then measure the arithmetic alone.  The one value test
+ * that decides the sample set, the early stop, can be handed to it from a
+ * float run (oracle_render's stop_in), so that it also stops where the float
+ * run stopped.
+ *
  * Two places where the reference's device code calls approximate hardware
  * functions are restated from their mathematical definition:
  *   - rnorm3df (svox2/csrc/include/cuda_util.cuh:87-92) -> 1/sqrt formed in double;
@@ -26,9 +37,10 @@
 #define CAT(a, b) CAT_(a, b)
 #define FN(name) CAT(name, SUFFIX)
 
+/* sampling geometry of a ray: float in both instances (see above) */
 typedef struct {
-  REAL o[3], d[3];
-  REAL world_step, tmin, tmax;
+  float o[3], d[3];
+  float world_step, tmin, tmax;
 } FN(ray_t);
 
 static REAL FN(lerp)(REAL a, REAL b, REAL w) { return FMA(w, b - a, a); }
@@ -72,6 +84,28 @@ static REAL FN(rnorm3)(REAL x, REAL y, REAL z) {
 
 static REAL FN(recip)(REAL d) { return (REAL)(1.0 / (double)d); }
 
+/* float forms of the two above, for the sampling geometry */
+static float FN(rnorm3g)(float x, float y, float z) {
+  double s = (double)x * (double)x + (double)y * (double)y + (double)z * (double)z;
+  return (float)(1.0 / sqrt(s));
+}
+
+static float FN(recipg)(float d) { return (float)(1.0 / (double)d); }
+
+/* ConcentricSpheresIntersector, render_util.cuh:546-576, in float (the spheric clip). */
+static int FN(sphere_hitg)(const float o[3], const float d[3], float r, float* out, int near) {
+  float dd = (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2];
+  float od = (o[0] * d[0] + o[1] * d[1]) + o[2] * d[2];
+  float oo = (o[0] * o[0] + o[1] * o[1]) + o[2] * o[2];
+  float q2a = 2 * dd, qb = 2 * od;
+  float f = qb * qb - (2 * q2a) * oo;
+  float det = f + ((2 * q2a) * r) * r;
+  if (det < 0) return 0;
+  float sq = sqrtf(det);
+  *out = near ? (-qb - sq) / q2a : (-qb + sq) / q2a;
+  return 1;
+}
+
 /* ConcentricSpheresIntersector, render_util.cuh:546-576. */
 static int FN(sphere_hit)(const REAL o[3], const REAL d[3], REAL r, REAL* out, int near) {
   REAL dd = (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2];
@@ -87,85 +121,84 @@ static int FN(sphere_hit)(const REAL o[3], const REAL d[3], REAL r, REAL* out, i
 }
 
 /* ray_find_bounds, render_util.cuh:578-628 (+ transform_coord, _get_delta_scale). */
-static void FN(find_bounds)(FN(ray_t) * r, const REAL org[3], const REAL dir[3], const oracle_grid_t* g,
+static void FN(find_bounds)(FN(ray_t) * r, const float org[3], const float dir[3], const oracle_grid_t* g,
                             const oracle_opt_t* opt) {
   int i;
   for (i = 0; i < 3; ++i) {
-    r->o[i] = FMA(org[i], (REAL)g->scaling[i], (REAL)g->offset[i]);
-    r->d[i] = dir[i] * (REAL)g->scaling[i];
+    r->o[i] = fmaf(org[i], g->scaling[i], g->offset[i]);
+    r->d[i] = dir[i] * g->scaling[i];
   }
-  REAL ds = FN(rnorm3)(r->d[0], r->d[1], r->d[2]);
+  float ds = FN(rnorm3g)(r->d[0], r->d[1], r->d[2]);
   for (i = 0; i < 3; ++i) r->d[i] = r->d[i] * ds;
-  r->world_step = ds * (REAL)opt->step;
+  r->world_step = ds * opt->step;
   if (opt->spheric) {
-    REAL so[3], sd[3];
+    float so[3], sd[3];
     for (i = 0; i < 3; ++i) {
-      REAL s = (REAL)2 / (REAL)g->size[i];
-      so[i] = FMA(r->o[i] + (REAL)0.5, s, (REAL)-1);
+      float s = 2.f / (float)g->size[i];
+      so[i] = fmaf(r->o[i] + 0.5f, s, -1.f);
       sd[i] = r->d[i] * s;
     }
-    if (!FN(sphere_hit)(so, sd, (REAL)1, &r->tmax, 0) ||
-        !FN(sphere_hit)(so, sd, (REAL)1 - (REAL)opt->near_clip, &r->tmin, 1)) {
-      r->tmin = (REAL)1e-9f;
+    if (!FN(sphere_hitg)(so, sd, 1.f, &r->tmax, 0) || !FN(sphere_hitg)(so, sd, 1.f - opt->near_clip, &r->tmin, 1)) {
+      r->tmin = 1e-9f;
       r->tmax = 0;
     }
   } else {
-    r->tmin = (REAL)opt->near_clip / r->world_step * (REAL)opt->step;
-    r->tmax = (REAL)2e3f;
+    r->tmin = opt->near_clip / r->world_step * opt->step;
+    r->tmax = 2e3f;
     for (i = 0; i < 3; ++i) {
-      REAL inv = FN(recip)(r->d[i]);
-      REAL t1 = ((REAL)-0.5 - r->o[i]) * inv;
-      REAL t2 = (((REAL)g->size[i] - (REAL)0.5) - r->o[i]) * inv;
+      float inv = FN(recipg)(r->d[i]);
+      float t1 = (-0.5f - r->o[i]) * inv;
+      float t2 = (((float)g->size[i] - 0.5f) - r->o[i]) * inv;
       if (r->d[i] != 0) {
-        r->tmin = FMAX(r->tmin, FMIN(t1, t2));
-        r->tmax = FMIN(r->tmax, FMAX(t1, t2));
+        r->tmin = fmaxf(r->tmin, fminf(t1, t2));
+        r->tmax = fminf(r->tmax, fmaxf(t1, t2));
       }
     }
   }
 }
 
 /* compute_skip_dist, render_util.cuh:235-295 (pos_offset = 0). */
-static REAL FN(skip_dist)(int32_t link, const int l[3], const REAL pos[3], const REAL d[3]) {
+static float FN(skip_dist)(int32_t link, const int l[3], const float pos[3], const float d[3]) {
   uint32_t dist = (uint32_t)(-link), shift = dist - 1u;
   uint32_t side = (uint32_t)((float)(1u << shift) - 1.f);
-  REAL tmin = 0, tmax = (REAL)1e9f;
+  float tmin = 0, tmax = 1e9f;
   int i;
   for (i = 0; i < 3; ++i) {
     int ul = ((l[i] >> shift) << shift) - l[i];
-    REAL inv = FN(recip)(d[i]);
-    REAL t1 = ((REAL)ul - pos[i]) * inv;
-    REAL t2 = ((REAL)((uint32_t)ul + side) - pos[i]) * inv;
+    float inv = FN(recipg)(d[i]);
+    float t1 = ((float)ul - pos[i]) * inv;
+    float t2 = ((float)((uint32_t)ul + side) - pos[i]) * inv;
     if (d[i] != 0) {
-      tmin = FMAX(tmin, FMIN(t1, t2));
-      tmax = FMIN(tmax, FMAX(t1, t2));
+      tmin = fmaxf(tmin, fminf(t1, t2));
+      tmax = fminf(tmax, fmaxf(t1, t2));
     }
   }
   return tmin > 0 ? 0 : tmax;
 }
 
 /* cam2world_ray + world2ndc, render_util.cuh:504-544.  c2w row-major, 4 columns. */
-static void FN(camera_ray)(int ix, int iy, const oracle_cam_t* cam, REAL dir[3], REAL org[3]) {
-  REAL x = (((REAL)ix + (REAL)0.5) - (REAL)cam->cx) / (REAL)cam->fx;
-  REAL y = (((REAL)iy + (REAL)0.5) - (REAL)cam->cy) / (REAL)cam->fy;
-  REAL z = SQRT((REAL)((double)(x * x + y * y) + 1.0));
+static void FN(camera_ray)(int ix, int iy, const oracle_cam_t* cam, float dir[3], float org[3]) {
+  float x = (((float)ix + 0.5f) - cam->cx) / cam->fx;
+  float y = (((float)iy + 0.5f) - cam->cy) / cam->fy;
+  float z = sqrtf((float)((double)(x * x + y * y) + 1.0));
   int r, i;
   x = x / z;
   y = y / z;
-  z = (REAL)1 / z;
+  z = 1.f / z;
   for (r = 0; r < 3; ++r) {
-    dir[r] = ((REAL)cam->c2w[4 * r] * x + (REAL)cam->c2w[4 * r + 1] * y) + (REAL)cam->c2w[4 * r + 2] * z;
-    org[r] = (REAL)cam->c2w[4 * r + 3];
+    dir[r] = (cam->c2w[4 * r] * x + cam->c2w[4 * r + 1] * y) + cam->c2w[4 * r + 2] * z;
+    org[r] = cam->c2w[4 * r + 3];
   }
   if (cam->ndcx > 0.f) {
-    REAL t = ((REAL)1 - org[2]) / dir[2];
-    for (i = 0; i < 3; ++i) org[i] = FMA(t, dir[i], org[i]);
-    dir[0] = (REAL)cam->ndcx * (dir[0] / dir[2] - org[0] / org[2]);
-    dir[1] = (REAL)cam->ndcy * (dir[1] / dir[2] - org[1] / org[2]);
-    dir[2] = (REAL)2 / org[2];
-    org[0] = (REAL)cam->ndcx * (org[0] / org[2]);
-    org[1] = (REAL)cam->ndcy * (org[1] / org[2]);
-    org[2] = (REAL)1 - (REAL)2 / org[2];
-    REAL rn = FN(rnorm3)(dir[0], dir[1], dir[2]);
+    float t = (1.f - org[2]) / dir[2];
+    for (i = 0; i < 3; ++i) org[i] = fmaf(t, dir[i], org[i]);
+    dir[0] = cam->ndcx * (dir[0] / dir[2] - org[0] / org[2]);
+    dir[1] = cam->ndcy * (dir[1] / dir[2] - org[1] / org[2]);
+    dir[2] = 2.f / org[2];
+    org[0] = cam->ndcx * (org[0] / org[2]);
+    org[1] = cam->ndcy * (org[1] / org[2]);
+    org[2] = 1.f - 2.f / org[2];
+    float rn = FN(rnorm3g)(dir[0], dir[1], dir[2]);
     for (i = 0; i < 3; ++i) dir[i] = dir[i] * rn;
   }
 }
@@ -175,23 +208,23 @@ static void FN(atomic_add)(REAL* p, REAL v) {
   *p += v;
 }
 
-/* Per-sample state of the march, shared by the forward and backward loops. */
+/* Per-sample state of the march, shared by the forward and backward loops (geometry: float). */
 typedef struct {
-  REAL pos[3];
+  float pos[3];
   int l[3];
   const int32_t* lp;
   int64_t base;
 } FN(sample_t);
 
-static void FN(locate)(const oracle_grid_t* g, const FN(ray_t) * r, REAL t, FN(sample_t) * s) {
+static void FN(locate)(const oracle_grid_t* g, const FN(ray_t) * r, float t, FN(sample_t) * s) {
   const int64_t offy = g->size[2], offx = (int64_t)g->size[1] * g->size[2];
   int j;
   for (j = 0; j < 3; ++j) {
-    REAL p = FMA(t, r->d[j], r->o[j]);
-    p = FMIN(FMAX(p, (REAL)0), (REAL)g->size[j] - (REAL)1);
+    float p = fmaf(t, r->d[j], r->o[j]);
+    p = fminf(fmaxf(p, 0.f), (float)g->size[j] - 1.f);
     s->l[j] = (int)p;
     if (s->l[j] > g->size[j] - 2) s->l[j] = g->size[j] - 2;
-    s->pos[j] = p - (REAL)s->l[j];
+    s->pos[j] = p - (float)s->l[j];
   }
   s->base = (int64_t)s->l[0] * offx + (int64_t)s->l[1] * offy + s->l[2];
   s->lp = g->links + s->base;
@@ -207,9 +240,10 @@ static REAL FN(trilerp)(const oracle_grid_t* g, const FN(sample_t) * s, const fl
     int32_t lk = s->lp[co[j]];
     v[j] = lk >= 0 ? (REAL)data[(int64_t)lk * stride + idx] : 0;
   }
-  REAL ix0 = FN(lerp)(FN(lerp)(v[0], v[1], s->pos[2]), FN(lerp)(v[2], v[3], s->pos[2]), s->pos[1]);
-  REAL ix1 = FN(lerp)(FN(lerp)(v[4], v[5], s->pos[2]), FN(lerp)(v[6], v[7], s->pos[2]), s->pos[1]);
-  return FN(lerp)(ix0, ix1, s->pos[0]);
+  const REAL p0 = (REAL)s->pos[0], p1 = (REAL)s->pos[1], p2 = (REAL)s->pos[2];
+  REAL ix0 = FN(lerp)(FN(lerp)(v[0], v[1], p2), FN(lerp)(v[2], v[3], p2), p1);
+  REAL ix1 = FN(lerp)(FN(lerp)(v[4], v[5], p2), FN(lerp)(v[6], v[7], p2), p1);
+  return FN(lerp)(ix0, ix1, p0);
 }
 
 /* Colour sum per channel group, before the +0.5 offset. */
@@ -220,16 +254,29 @@ static void FN(sample_colour)(const oracle_grid_t* g, const FN(sample_t) * s, co
   for (c = 0; c < C; ++c) col[c / bd] += FN(trilerp)(g, s, g->sh, C, c) * basis[c % bd];
 }
 
+/* Early stop of a ray: stop_in < -1 takes the ray's own test (log T below the
+ * threshold's log); stop_in == -1 never stops; stop_in = n >= 1 stops right after the
+ * ray's n-th evaluated sample.  The last two replay a float run's stops (reported
+ * through stop_out) in the double instance. */
+static int FN(stops)(int stop_in, REAL lt, REAL log_stop, int n_done) {
+  if (stop_in < -1) return lt < log_stop;
+  return stop_in >= 0 && n_done >= stop_in;
+}
+
 /* trace_ray_cuvol, render_lerp_kernel_cuvol.cu:30-120.  Returns the colour and
- * the log transmittance the reference reports (-1e3 after an early stop). */
-static void FN(fwd_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const REAL org[3], const REAL dir[3],
-                        REAL out[3], REAL* log_t, uint64_t* trace, uint64_t* n_eval) {
-  const REAL log_stop = FN(log_stop)(opt->stop_thresh), step = (REAL)opt->step;
-  REAL basis[9], outv[3] = {0, 0, 0}, t, lt = 0, ws;
+ * the log transmittance the reference reports (-1e3 after an early stop).
+ * *stop_out: the ray's evaluated-sample count at its early stop, or -1. */
+static void FN(fwd_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const float org[3], const float dir[3],
+                        REAL out[3], REAL* log_t, uint64_t* trace, uint64_t* n_eval, int stop_in, int* stop_out) {
+  const REAL log_stop = FN(log_stop)(opt->stop_thresh);
+  const float step = opt->step;
+  REAL basis[9], dr[3] = {dir[0], dir[1], dir[2]}, outv[3] = {0, 0, 0}, lt = 0;
+  float t, ws;
   FN(ray_t) r;
   uint64_t h = 1469598103934665603ull;
-  int c;
-  FN(calc_sh)(g->basis_dim, dir, basis);
+  int c, ne = 0;
+  if (stop_out) *stop_out = -1;
+  FN(calc_sh)(g->basis_dim, dr, basis);
   FN(find_bounds)(&r, org, dir, g, opt);
   if (r.tmin > r.tmax) {
     for (c = 0; c < 3; ++c) out[c] = g->bg_nlayers == 0 ? (REAL)opt->bg : (REAL)0;
@@ -243,28 +290,30 @@ static void FN(fwd_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const R
     FN(sample_t) s;
     FN(locate)(g, &r, t, &s);
     if (s.lp[0] < -1) {
-      REAL skip = FN(skip_dist)(s.lp[0], s.l, s.pos, r.d);
+      float skip = FN(skip_dist)(s.lp[0], s.l, s.pos, r.d);
       if (skip >= step) {
         h = ((h ^ (uint64_t)s.base) * 1099511628211ull ^ 3ull) * 1099511628211ull;
-        t = t + CEIL(skip / step) * step;
+        t = t + ceilf(skip / step) * step;
         continue;
       }
     }
     REAL sigma = FN(trilerp)(g, &s, g->density, 1, 0);
-    if (opt->last_opaque && t + step > r.tmax) ws = (REAL)1e9f;
+    if (opt->last_opaque && t + step > r.tmax) ws = 1e9f;
     const int ev = sigma > (REAL)opt->sigma_thresh;
     h = (h ^ (uint64_t)s.base) * 1099511628211ull;
     h = (h ^ (ev ? 1ull : 2ull)) * 1099511628211ull;
     if (ev) {
       REAL col[3];
       FN(sample_colour)(g, &s, basis, col);
-      const REAL pcnt = ws * sigma;
+      const REAL pcnt = (REAL)ws * sigma;
       const REAL w = EXP(lt) * ((REAL)1 - EXP(-pcnt));
       lt = lt - pcnt;
       ++*n_eval;
+      ++ne;
       for (c = 0; c < 3; ++c) outv[c] = outv[c] + w * FMAX(col[c] + (REAL)0.5, (REAL)0);
-      if (lt < log_stop) {
+      if (FN(stops)(stop_in, lt, log_stop, ne)) {
         lt = (REAL)-1e3f;
+        if (stop_out) *stop_out = ne;
         break;
       }
     }
@@ -279,18 +328,28 @@ static void FN(fwd_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const R
 /* trace_ray_cuvol_backward, render_lerp_kernel_cuvol.cu:227-383, forward order:
  * accum starts at dot(colour, gout) and loses each sample's contribution.  Reports the
  * accum left after the last sample (beta term taken out) and the log transmittance there,
- * which the MSI background's backward starts from (cuvol.cu:253-258, 374-383). */
-static void FN(bwd_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const REAL org[3], const REAL dir[3],
+ * which the MSI background's backward starts from (cuvol.cu:253-258, 374-383).
+ * mag_density / mag_sh (optional) receive, per gradient entry, the scale against which
+ * float arithmetic loses precision: the sum over its terms of |term| * F, the density term
+ * counting its two parts |tc T_after| and the ray's total light A = sum_c |gout_c colour_c|
+ * + |beta term| (an upper bound on |accum|) separately.  F = 1 + sum of |log T| over the
+ * ray's samples so far bounds, in units of the float rounding unit, the rounding error that
+ * the float chain of log T subtractions has built up by then: every later weight and
+ * transmittance inherits it as a relative error. */
+static void FN(bwd_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const float org[3], const float dir[3],
                         const REAL color[3], REAL log_t_in, const REAL gout[3], REAL beta_loss, REAL sparsity,
-                        REAL* grad_density, REAL* grad_sh, uint8_t* mask, REAL* accum_out, REAL* log_t_out) {
+                        REAL* grad_density, REAL* grad_sh, uint8_t* mask, REAL* accum_out, REAL* log_t_out,
+                        int stop_in, REAL* mag_density, REAL* mag_sh) {
   const int bd = g->basis_dim, C = 3 * bd;
   const int64_t offy = g->size[2], offx = (int64_t)g->size[1] * g->size[2];
   const int64_t co[8] = {0, 1, offy, offy + 1, offx, offx + 1, offx + offy, offx + offy + 1};
-  const REAL log_stop = FN(log_stop)(opt->stop_thresh), step = (REAL)opt->step;
-  REAL basis[9], t, lt = 0, ws, accum, beta_term = 0;
+  const REAL log_stop = FN(log_stop)(opt->stop_thresh);
+  const float step = opt->step;
+  REAL basis[9], dr[3] = {dir[0], dir[1], dir[2]}, lt = 0, accum, beta_term = 0, amag, fchain = 1;
+  float t, ws;
   FN(ray_t) r;
-  int c, j;
-  FN(calc_sh)(bd, dir, basis);
+  int c, j, ne = 0;
+  FN(calc_sh)(bd, dr, basis);
   FN(find_bounds)(&r, org, dir, g, opt);
   accum = FMA(color[0], gout[0], FMA(color[1], gout[1], color[2] * gout[2]));
   *accum_out = accum;
@@ -301,26 +360,28 @@ static void FN(bwd_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const R
     beta_term = (REAL)((double)beta_loss * (1.0 - (double)tin / ((double)((REAL)1 - tin) + 1e-3)));
     accum += beta_term;
   }
+  amag = (FABS(color[0] * gout[0]) + FABS(color[1] * gout[1])) + FABS(color[2] * gout[2]) + FABS(beta_term);
   t = r.tmin;
   ws = r.world_step;
   while (t <= r.tmax) {
     FN(sample_t) s;
     FN(locate)(g, &r, t, &s);
     if (s.lp[0] < -1) {
-      REAL skip = FN(skip_dist)(s.lp[0], s.l, s.pos, r.d);
+      float skip = FN(skip_dist)(s.lp[0], s.l, s.pos, r.d);
       if (skip >= step) {
-        t = t + CEIL(skip / step) * step;
+        t = t + ceilf(skip / step) * step;
         continue;
       }
     }
     REAL sigma = FN(trilerp)(g, &s, g->density, 1, 0);
-    if (opt->last_opaque && t + step > r.tmax) ws = (REAL)1e9f;
+    if (opt->last_opaque && t + step > r.tmax) ws = 1e9f;
     if (sigma > (REAL)opt->sigma_thresh) {
-      REAL col[3], tot[3], in01[3], wts[8];
+      REAL col[3], tot[3], in01[3], wts[8], gsp = 0;
       FN(sample_colour)(g, &s, basis, col);
-      const REAL pcnt = ws * sigma;
+      const REAL pcnt = (REAL)ws * sigma;
       const REAL w = EXP(lt) * ((REAL)1 - EXP(-pcnt));
       lt = lt - pcnt;
+      ++ne;
       for (c = 0; c < 3; ++c) {
         const REAL lc = col[c] + (REAL)0.5;
         const REAL tc = FMAX(lc, (REAL)0);
@@ -328,22 +389,28 @@ static void FN(bwd_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const R
         tot[c] = tc * gout[c];
       }
       const REAL tcs = (tot[0] + tot[2]) + tot[1];
+      const REAL tn = EXP(lt);
+      fchain += FABS(lt);
       accum = accum - w * tcs;
-      REAL gsig = ws * (tcs * EXP(lt) - accum);
-      if (sparsity > 0) gsig += sparsity * ((REAL)4 * sigma / ((REAL)1 + (REAL)2 * (sigma * sigma)));
+      REAL gsig = (REAL)ws * (tcs * tn - accum);
+      if (sparsity > 0) {
+        gsp = sparsity * ((REAL)4 * sigma / ((REAL)1 + (REAL)2 * (sigma * sigma)));
+        gsig += gsp;
+      }
       /* trilerp_backward_cuvol_one(_density), render_util.cuh:94-153 */
       {
-        const REAL ay = (REAL)1 - s.pos[1], az = (REAL)1 - s.pos[2];
-        REAL xo = (REAL)1 - s.pos[0];
+        const REAL p0 = (REAL)s.pos[0], p1 = (REAL)s.pos[1], p2 = (REAL)s.pos[2];
+        const REAL ay = (REAL)1 - p1, az = (REAL)1 - p2;
+        REAL xo = (REAL)1 - p0;
         wts[0] = ay * az * xo;
-        wts[1] = ay * s.pos[2] * xo;
-        wts[2] = s.pos[1] * az * xo;
-        wts[3] = s.pos[1] * s.pos[2] * xo;
-        xo = s.pos[0];
+        wts[1] = ay * p2 * xo;
+        wts[2] = p1 * az * xo;
+        wts[3] = p1 * p2 * xo;
+        xo = p0;
         wts[4] = ay * az * xo;
-        wts[5] = ay * s.pos[2] * xo;
-        wts[6] = s.pos[1] * az * xo;
-        wts[7] = s.pos[1] * s.pos[2] * xo;
+        wts[5] = ay * p2 * xo;
+        wts[6] = p1 * az * xo;
+        wts[7] = p1 * p2 * xo;
       }
       for (j = 0; j < 8; ++j) {
         const int32_t lk = s.lp[co[j]];
@@ -352,9 +419,16 @@ static void FN(bwd_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const R
           for (c = 0; c < C; ++c)
             FN(atomic_add)(grad_sh + (int64_t)lk * C + c, wts[j] * (basis[c % bd] * (w * in01[c / bd] * gout[c / bd])));
         if (grad_density) FN(atomic_add)(grad_density + lk, wts[j] * gsig);
+        if (mag_sh)
+          for (c = 0; c < C; ++c)
+            FN(atomic_add)(mag_sh + (int64_t)lk * C + c,
+                           fchain * FABS(wts[j] * (basis[c % bd] * (w * in01[c / bd] * gout[c / bd]))));
+        if (mag_density)
+          FN(atomic_add)(mag_density + lk,
+                         fchain * wts[j] * ((REAL)ws * (FABS(tcs * tn) + amag) + FABS(gsp)));
         if (mask) mask[lk] = 1;
       }
-      if (lt < log_stop) break;
+      if (FN(stops)(stop_in, lt, log_stop, ne)) break;
     }
     t = t + step;
   }
@@ -572,47 +646,58 @@ void FN(oracle_msi_tv_grad)(const int32_t* links, int size0, int size1, const fl
  * (render_lerp_kernel_cuvol.cu:918-958, 1070-1152, 1010-1068).
  *   mode 0: forward, rgb_out written.
  *   mode 1: fused MSE: forward into rgb_out, gout = (rgb_out - rgb_gt) * 2/(3Q), backward.
- *   mode 2: backward with grad_out; rgb_out must hold the forward colour (color_cache). */
+ *   mode 2: backward with grad_out; rgb_out must hold the forward colour (color_cache).
+ * stop_out (optional) receives each ray's early-stop count (-1: no early stop); stop_in
+ * (optional) makes every ray stop where such a record says instead of by its own test.
+ * mag_density / mag_sh (optional): the per-entry magnitudes of bwd_ray. */
 void FN(oracle_render)(const oracle_grid_t* g, const oracle_opt_t* opt, const float* origins, const float* dirs,
                        int64_t Q, int mode, const float* rgb_gt, const float* grad_out, float beta_loss,
                        float sparsity, REAL* rgb_out, REAL* grad_density, REAL* grad_sh, uint8_t* mask,
                        REAL* grad_bg, uint8_t* mask_bg, uint64_t* trace, uint64_t* n_eval_total,
-                       uint64_t* n_bg_total, int nthreads) {
+                       uint64_t* n_bg_total, int nthreads, int32_t* stop_out, const int32_t* stop_in,
+                       REAL* mag_density, REAL* mag_sh) {
   int64_t q;
   uint64_t total = 0, total_bg = 0;
   const REAL norm = (REAL)2.f / (REAL)(float)(3 * Q);
   if (nthreads < 1) nthreads = 1;
 #pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads) reduction(+ : total, total_bg)
   for (q = 0; q < Q; ++q) {
-    REAL org[3], dir[3], out[3], gout[3], lt = 0, acc_b = 0, lt_b = 0;
+    float org[3], dir[3];
+    REAL orgr[3], dirr[3], out[3], gout[3], lt = 0, acc_b = 0, lt_b = 0;
     const int bg = g->bg_nlayers > 0;
+    const int sin_ = stop_in ? stop_in[q] : -2;
     uint64_t ne = 0, nb = 0;
-    int i;
+    int i, so = -1;
     for (i = 0; i < 3; ++i) {
-      org[i] = (REAL)origins[q * 3 + i];
-      dir[i] = (REAL)dirs[q * 3 + i];
+      org[i] = origins[q * 3 + i];
+      dir[i] = dirs[q * 3 + i];
+      orgr[i] = (REAL)org[i];
+      dirr[i] = (REAL)dir[i];
     }
     if (mode == 0 || mode == 1) {
-      FN(fwd_ray)(g, opt, org, dir, out, &lt, trace ? trace + q : NULL, &ne);
+      FN(fwd_ray)(g, opt, org, dir, out, &lt, trace ? trace + q : NULL, &ne, sin_, &so);
       /* render_background_kernel skips rays whose log transmittance is below -25 */
-      if (bg && lt >= (REAL)-25) FN(bg_ray)(g, opt, org, dir, lt, NULL, 0, 0, out, NULL, NULL, &nb);
+      if (bg && lt >= (REAL)-25) FN(bg_ray)(g, opt, orgr, dirr, lt, NULL, 0, 0, out, NULL, NULL, &nb);
       for (i = 0; i < 3; ++i) rgb_out[q * 3 + i] = out[i];
+      if (stop_out) stop_out[q] = so;
     }
     if (mode == 1) {
       for (i = 0; i < 3; ++i) gout[i] = (out[i] - (REAL)rgb_gt[q * 3 + i]) * norm;
       FN(bwd_ray)(g, opt, org, dir, out, lt, gout, (REAL)beta_loss / (REAL)Q, (REAL)sparsity, grad_density,
-                  grad_sh, mask, &acc_b, &lt_b);
+                  grad_sh, mask, &acc_b, &lt_b, sin_, mag_density, mag_sh);
       /* the fused path's background backward starts from the forward's log transmittance */
       if (bg && lt >= (REAL)-25)
-        FN(bg_ray)(g, opt, org, dir, lt, gout, acc_b, (REAL)sparsity, NULL, grad_bg, mask_bg, NULL);
+        FN(bg_ray)(g, opt, orgr, dirr, lt, gout, acc_b, (REAL)sparsity, NULL, grad_bg, mask_bg, NULL);
     } else if (mode == 2) {
       for (i = 0; i < 3; ++i) {
         out[i] = rgb_out[q * 3 + i];
         gout[i] = (REAL)grad_out[q * 3 + i];
       }
-      FN(bwd_ray)(g, opt, org, dir, out, 0, gout, 0, 0, grad_density, grad_sh, NULL, &acc_b, &lt_b);
+      FN(bwd_ray)(g, opt, org, dir, out, 0, gout, 0, 0, grad_density, grad_sh, NULL, &acc_b, &lt_b, sin_,
+                  mag_density, mag_sh);
       /* volume_render_cuvol_backward: from the backward pass's own log transmittance */
-      if (bg && lt_b >= (REAL)-25) FN(bg_ray)(g, opt, org, dir, lt_b, gout, acc_b, 0, NULL, grad_bg, NULL, NULL);
+      if (bg && lt_b >= (REAL)-25)
+        FN(bg_ray)(g, opt, orgr, dirr, lt_b, gout, acc_b, 0, NULL, grad_bg, NULL, NULL);
     }
     total += ne;
     total_bg += nb;
@@ -625,10 +710,11 @@ void FN(oracle_render)(const oracle_grid_t* g, const oracle_opt_t* opt, const fl
  * (178-225): the expected termination distance sum w * (t / step) * world_step, or
  * (threshold) the distance (t / step) * world_step of the first sample with sigma >
  * sigma_thresh.  Neither applies last_sample_opaque. */
-static REAL FN(depth_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const REAL org[3], const REAL dir[3],
+static REAL FN(depth_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const float org[3], const float dir[3],
                           int threshold, float sigma_thresh) {
   const REAL log_stop = FN(log_stop)(opt->stop_thresh), step = (REAL)opt->step;
-  REAL t, lt = 0, outv = 0;
+  REAL lt = 0, outv = 0;
+  float t;
   FN(ray_t) r;
   FN(find_bounds)(&r, org, dir, g, opt);
   if (r.tmin > r.tmax) return 0;
@@ -637,25 +723,25 @@ static REAL FN(depth_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const
     FN(sample_t) s;
     FN(locate)(g, &r, t, &s);
     if (s.lp[0] < -1) {
-      REAL skip = FN(skip_dist)(s.lp[0], s.l, s.pos, r.d);
-      if (skip >= step) {
-        t = t + CEIL(skip / step) * step;
+      float skip = FN(skip_dist)(s.lp[0], s.l, s.pos, r.d);
+      if (skip >= opt->step) {
+        t = t + ceilf(skip / opt->step) * opt->step;
         continue;
       }
     }
     {
       const REAL sigma = FN(trilerp)(g, &s, g->density, 1, 0);
       if (threshold) {
-        if (sigma > (REAL)sigma_thresh) return (t / step) * r.world_step;
+        if (sigma > (REAL)sigma_thresh) return ((REAL)t / step) * (REAL)r.world_step;
       } else if (sigma > (REAL)opt->sigma_thresh) {
-        const REAL pcnt = r.world_step * sigma;
+        const REAL pcnt = (REAL)r.world_step * sigma;
         const REAL w = EXP(lt) * ((REAL)1 - EXP(-pcnt));
         lt = lt - pcnt;
-        outv = outv + w * (t / step) * r.world_step;
+        outv = outv + w * ((REAL)t / step) * (REAL)r.world_step;
         if (lt < log_stop) break;
       }
     }
-    t = t + step;
+    t = t + opt->step;
   }
   return outv;
 }
@@ -667,11 +753,11 @@ void FN(oracle_render_depth)(const oracle_grid_t* g, const oracle_opt_t* opt, co
   if (nthreads < 1) nthreads = 1;
 #pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads)
   for (q = 0; q < Q; ++q) {
-    REAL org[3], dir[3];
+    float org[3], dir[3];
     int i;
     for (i = 0; i < 3; ++i) {
-      org[i] = (REAL)origins[q * 3 + i];
-      dir[i] = (REAL)dirs[q * 3 + i];
+      org[i] = origins[q * 3 + i];
+      dir[i] = dirs[q * 3 + i];
     }
     out[q] = FN(depth_ray)(g, opt, org, dir, threshold, sigma_thresh);
   }
@@ -686,7 +772,7 @@ void FN(oracle_grid_weight_render)(const float* data, const int size[3], const o
                                    const float scaling[3], REAL* wmax) {
   oracle_grid_t g;
   oracle_opt_t opt;
-  const REAL log_stop = FN(log_stop)(stop_thresh), step = (REAL)step_size;
+  const REAL log_stop = FN(log_stop)(stop_thresh);
   const int64_t offy = size[2], offx = (int64_t)size[1] * size[2];
   const int64_t co[8] = {0, 1, offy, offy + 1, offx, offx + 1, offx + offy, offx + offy + 1};
   int64_t q, n = (int64_t)cam->width * cam->height;
@@ -709,7 +795,8 @@ void FN(oracle_grid_weight_render)(const float* data, const int size[3], const o
   opt.spheric = 0;
   opt.last_opaque = last_opaque;
   for (q = 0; q < n; ++q) {
-    REAL org[3], dir[3], t, ll = 0;
+    float org[3], dir[3], t;
+    REAL ll = 0;
     FN(ray_t) r;
     FN(camera_ray)((int)(q % cam->width), (int)(q / cam->width), cam, dir, org);
     FN(find_bounds)(&r, org, dir, &g, &opt);
@@ -720,29 +807,29 @@ void FN(oracle_grid_weight_render)(const float* data, const int size[3], const o
       int l[3], j;
       int64_t idx;
       for (j = 0; j < 3; ++j) {
-        REAL p = FMA(t, r.d[j], r.o[j]);
-        p = FMIN(FMAX(p, (REAL)0), (REAL)size[j] - (REAL)1);
+        float p = fmaf(t, r.d[j], r.o[j]);
+        p = fminf(fmaxf(p, 0.f), (float)size[j] - 1.f);
         l[j] = (int)p;
         if (l[j] > size[j] - 2) l[j] = size[j] - 2;
-        pos[j] = p - (REAL)l[j];
+        pos[j] = (REAL)(p - (float)l[j]);
       }
       idx = (int64_t)l[0] * offx + (int64_t)l[1] * offy + l[2];
       for (j = 0; j < 8; ++j) v[j] = (REAL)data[idx + co[j]];
       sigma = FN(lerp)(FN(lerp)(FN(lerp)(v[0], v[1], pos[2]), FN(lerp)(v[2], v[3], pos[2]), pos[1]),
                        FN(lerp)(FN(lerp)(v[4], v[5], pos[2]), FN(lerp)(v[6], v[7], pos[2]), pos[1]), pos[0]);
-      if (last_opaque && t + step > r.tmax) {
+      if (last_opaque && t + step_size > r.tmax) {
         sigma = sigma + (REAL)1e9f;
         ll = 0;
       }
       if (sigma > (REAL)1e-8f) {
-        const REAL la = -(r.world_step * sigma);
+        const REAL la = -((REAL)r.world_step * sigma);
         const REAL w = EXP(ll) * ((REAL)1 - EXP(la));
         ll = ll + la;
         for (j = 0; j < 8; ++j)
           if (w > wmax[idx + co[j]]) wmax[idx + co[j]] = w;
         if (ll < log_stop) break;
       }
-      t = t + step;
+      t = t + step_size;
     }
   }
 }
@@ -754,12 +841,18 @@ void FN(oracle_render_image)(const oracle_grid_t* g, const oracle_opt_t* opt, co
   if (nthreads < 1) nthreads = 1;
 #pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads)
   for (q = 0; q < n; ++q) {
-    REAL org[3], dir[3], rgb[3], lt;
+    float org[3], dir[3];
+    REAL orgr[3], dirr[3], rgb[3], lt;
     uint64_t ne = 0;
     int i;
     FN(camera_ray)((int)(q % cam->width), (int)(q / cam->width), cam, dir, org);
-    FN(fwd_ray)(g, opt, org, dir, rgb, &lt, trace ? trace + q : NULL, &ne);
-    if (g->bg_nlayers > 0 && lt >= (REAL)-25) FN(bg_ray)(g, opt, org, dir, lt, NULL, 0, 0, rgb, NULL, NULL, NULL);
+    FN(fwd_ray)(g, opt, org, dir, rgb, &lt, trace ? trace + q : NULL, &ne, -2, NULL);
+    for (i = 0; i < 3; ++i) {
+      orgr[i] = (REAL)org[i];
+      dirr[i] = (REAL)dir[i];
+    }
+    if (g->bg_nlayers > 0 && lt >= (REAL)-25)
+      FN(bg_ray)(g, opt, orgr, dirr, lt, NULL, 0, 0, rgb, NULL, NULL, NULL);
     for (i = 0; i < 3; ++i) out[q * 3 + i] = rgb[i];
   }
 }

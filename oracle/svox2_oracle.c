@@ -46,6 +46,7 @@ typedef struct {
 #define NEXTAFTER nextafterf
 #define ASIN asinf
 #define ATAN2 atan2f
+#define FABS fabsf
 #include "oracle_impl.h"
 #undef REAL
 #undef SUFFIX
@@ -58,6 +59,7 @@ typedef struct {
 #undef NEXTAFTER
 #undef ASIN
 #undef ATAN2
+#undef FABS
 
 #define REAL double
 #define SUFFIX _f64
@@ -70,6 +72,7 @@ typedef struct {
 #define NEXTAFTER nextafter
 #define ASIN asin
 #define ATAN2 atan2
+#define FABS fabs
 #include "oracle_impl.h"
 
 /* accel_dist_prop, svox2/csrc/misc_kernel.cu:108-181 (kernels) and 356-416 (host):

@@ -587,19 +587,26 @@ extern "C" int svx_color_cache_capacity(void) { return svx::g_cap; }
 //
 // The array is kStaticScratchWords 64-bit words (256 bytes).  Every GPU that
 // loads this library holds one copy of it until the process exits.  A call
-// needs one word; the entry rejects any request for more scratch than the
-// array holds.  All calls share the array and it keeps the last call's
-// contents: each call clears the counter on its stream before the kernel
-// starts, so calls that overlap on the GPU (on different streams, or from
-// different host threads) race on the counter and must be serialised by the
-// caller.
+// needs kNoallocWords of it whatever its size (the counter does not grow with
+// the rays or the grid), which the static_assert below holds to the array.
+// All calls share the array and it keeps the last call's contents: each call
+// clears the counter on its stream before the kernel starts, so calls that
+// overlap on the GPU (on different streams, or from different host threads)
+// race on the counter and must be serialised by the caller.
 constexpr int kStaticScratchWords = 32;
+constexpr int kNoallocWords = 1;  // the ray counter
+static_assert(kNoallocWords <= kStaticScratchWords, "the allocation-free render's scratch must fit the array");
 static __device__ __align__(256) unsigned long long g_static_scratch[kStaticScratchWords];
 
-// Device address of g_static_scratch on the current device, looked up once
-// per device (with that device current) and cached.  In host code the
-// symbol's name is only a host-side stand-in; the kernel must be given the
-// address cudaGetSymbolAddress returns.
+// Device address of g_static_scratch on the current device, looked up with
+// that device current and cached per device.  In host code the symbol's name
+// is only a host-side stand-in; the kernel must be given the address
+// cudaGetSymbolAddress returns.  The address belongs to the context that was
+// current when it was looked up (the runtime's primary context of the
+// device): a cached address is checked against the current context with
+// cudaPointerGetAttributes on every call and looked up again when that no
+// longer reports it as this device's memory (after cudaDeviceReset, or under
+// another context).
 static int static_scratch_address(unsigned long long** out) {
   static std::mutex mu;
   static unsigned long long* addr[64] = {nullptr};
@@ -607,6 +614,12 @@ static int static_scratch_address(unsigned long long** out) {
   SVX_CUDA_TRY(cudaGetDevice(&dev));
   SVX_REQUIRE(dev >= 0 && dev < 64, SVX_ERR_UNSUPPORTED, "device index %d: at most 64 devices", dev);
   std::lock_guard<std::mutex> lk(mu);
+  if (addr[dev] != nullptr) {
+    cudaPointerAttributes at{};
+    const cudaError_t e = cudaPointerGetAttributes(&at, addr[dev]);
+    if (e != cudaSuccess) (void)cudaGetLastError();  // a failed query must not reach the launch check
+    if (e != cudaSuccess || at.type != cudaMemoryTypeDevice || at.device != dev) addr[dev] = nullptr;
+  }
   if (addr[dev] == nullptr) {
     void* p = nullptr;
     SVX_CUDA_TRY(cudaGetSymbolAddress(&p, g_static_scratch));
@@ -640,9 +653,6 @@ extern "C" int svx_volume_render_cuvol_fused_noalloc(const svx_grid_t* grid, con
   SVX_REQUIRE(max_samples <= (double)kNumCkpt * kMaxStride, SVX_ERR_TOO_LARGE,
               "up to %.0f samples per ray (grid diagonal / step_size); the adjoint supports %d", max_samples,
               kNumCkpt * kMaxStride);
-  const int need_words = 1;  // the ray counter
-  SVX_REQUIRE(need_words <= kStaticScratchWords, SVX_ERR_TOO_LARGE,
-              "needs %d words of static scratch, the array holds %d", need_words, kStaticScratchWords);
   unsigned long long* scratch = nullptr;
   rc = static_scratch_address(&scratch);
   if (rc) return rc;

@@ -734,38 +734,41 @@ class SparseGrid(nn.Module):
             indexer = torch.empty((0, 0), dtype=torch.bool, device=self.density_data.device)
         return indexer
 
+    @staticmethod
+    def _tv_cells(n_cells: int, sparse_frac: float, contiguous: bool, device) -> torch.Tensor:
+        """int32 indices of max(int(sparse_frac * n_cells), 1) cells for a sparse TV term: a
+        window of consecutive cells that wraps past the last one, starting at a cell drawn
+        from numpy's global RNG, or (contiguous False) cells drawn uniformly by torch on the
+        device.  The draws are the reference's (svox2/svox2.py:2224-2260), so a seeded run
+        selects the same cells."""
+        count = max(int(sparse_frac * n_cells), 1)
+        if not contiguous:
+            return torch.randint(0, n_cells, (count,), dtype=torch.int32, device=device)
+        first = np.random.randint(0, n_cells)
+        window = torch.arange(count, dtype=torch.int64, device=device).add_(first).remainder_(n_cells)
+        return window.to(torch.int32)
+
+    def _require_mask_state(self, indexer, what: str):
+        if indexer is not None and indexer.dtype != torch.bool:
+            raise AssertionError(f"{what} must come between the render that marks the touched cells and the "
+                                 "optimiser step that consumes the mark")
+
     def _get_rand_cells_background(self, sparse_frac: float, contiguous: bool = True):
-        """Random MSI background TV cells over the [2 reso, reso, nlayers] cells, drawn as
-        _get_rand_cells draws them (svox2/svox2.py:2243-2260)."""
-        assert self.use_background, "Can only use sparse background loss if using background"
-        assert self.sparse_background_indexer is None or self.sparse_background_indexer.dtype == torch.bool, \
-            "please call sparse loss after rendering and before gradient updates"
-        grid_size = self.background_links.size(0) * self.background_links.size(1) * self.background_data.size(1)
-        sparse_num = max(int(sparse_frac * grid_size), 1)
-        if contiguous:
-            start = np.random.randint(0, grid_size)
-            arr = torch.arange(start, start + sparse_num, dtype=torch.int32, device=self.links.device)
-            if start > grid_size - sparse_num:
-                arr[grid_size - sparse_num - start:] -= grid_size
-            return arr
-        return torch.randint(0, grid_size, (sparse_num,), dtype=torch.int32, device=self.links.device)
+        """Random cells of the MSI background's [2 reso, reso, nlayers] (cell, layer) table for
+        its TV term (svox2/svox2.py:2243-2260)."""
+        if not self.use_background:
+            raise AssertionError("this grid has no MSI background to regularise")
+        self._require_mask_state(self.sparse_background_indexer, "the background TV term")
+        n_cells = self.background_links.numel() * self.background_data.size(1)
+        return self._tv_cells(n_cells, sparse_frac, contiguous, self.links.device)
 
     def _get_rand_cells(self, sparse_frac: float, force: bool = False, contiguous: bool = True):
-        """Random TV cells: a contiguous (wrapping) window of max(int(frac * n), 1) cells from a
-        host RNG start (svox2/svox2.py:2224-2241), or uniform cells if not contiguous."""
-        if sparse_frac < 1.0 or force:
-            assert self.sparse_grad_indexer is None or self.sparse_grad_indexer.dtype == torch.bool, \
-                "please call sparse loss after rendering and before gradient updates"
-            grid_size = self.links.size(0) * self.links.size(1) * self.links.size(2)
-            sparse_num = max(int(sparse_frac * grid_size), 1)
-            if contiguous:
-                start = np.random.randint(0, grid_size)
-                arr = torch.arange(start, start + sparse_num, dtype=torch.int32, device=self.links.device)
-                if start > grid_size - sparse_num:
-                    arr[grid_size - sparse_num - start:] -= grid_size
-                return arr
-            return torch.randint(0, grid_size, (sparse_num,), dtype=torch.int32, device=self.links.device)
-        return None
+        """Random grid cells for a sparse TV term (svox2/svox2.py:2224-2241), or None for the
+        dense term (sparse_frac >= 1 and not force)."""
+        if sparse_frac >= 1.0 and not force:
+            return None
+        self._require_mask_state(self.sparse_grad_indexer, "a sparse TV term")
+        return self._tv_cells(self.links.numel(), sparse_frac, contiguous, self.links.device)
 
     # ---- depth renders (svox2/svox2.py:1181-1221)
     def volume_render_depth(self, rays: Rays, sigma_thresh: Optional[float] = None):
@@ -926,26 +929,29 @@ class SparseGrid(nn.Module):
 
     def sparsify_background(self, sigma_thresh: float = 1.0, dilate: int = 1):
         """Drop the MSI background cells whose sigma stays below sigma_thresh in every layer,
-        after `dilate` 3x3x3 dilations of the kept (cell, layer) mask, and re-index the rest in
-        raster order (svox2/svox2.py:1426-1448)."""
-        assert self.use_background, "the grid has no MSI background"
+        after `dilate` 3x3x3 dilations of the kept (cell, layer) mask, and number the rest in
+        raster order (svox2/svox2.py:1426-1448).  Each cell's layers are read through its own
+        link."""
+        if not self.use_background:
+            raise AssertionError("this grid has no MSI background to sparsify")
         if int(dilate) > 0 and not self.background_links.is_cuda:
             raise RuntimeError("sparsify_background dilates with a CUDA kernel: the grid must be on a CUDA device")
-        device = self.background_links.device
-        nl = self.background_nlayers
-        sigma_mask = torch.zeros(list(self.background_links.shape) + [nl], dtype=torch.bool,
-                                 device=device).view(-1, nl)
-        nonempty_mask = self.background_links.view(-1) >= 0
-        data_mask = self.background_data[..., -1] >= sigma_thresh
-        sigma_mask[nonempty_mask] = data_mask   # the rows in raster order of the non-empty cells
-        sigma_mask = sigma_mask.view(list(self.background_links.shape) + [nl])
+        links = self.background_links
+        device = links.device
+        rows = links.reshape(-1).long()
+        present = rows >= 0
+        dense = self.background_data[..., -1] >= sigma_thresh          # [rows, nlayers]
+        keep = torch.zeros((rows.numel(), dense.size(1)), dtype=torch.bool, device=device)
+        keep[present] = dense[rows[present]]
+        keep = keep.view(*links.shape, dense.size(1))
         for _ in range(int(dilate)):
-            sigma_mask = _C.dilate(sigma_mask)
-        sigma_mask = sigma_mask.any(-1) & nonempty_mask.view(self.background_links.shape)
-        self.background_links[~sigma_mask] = -1
-        retain_vals = self.background_links[sigma_mask]
-        self.background_links[sigma_mask] = torch.arange(retain_vals.size(0), dtype=torch.int32, device=device)
-        self.background_data = nn.Parameter(self.background_data.data[retain_vals.long()])
+            keep = _C.dilate(keep)
+        kept_cells = keep.any(-1).reshape(-1) & present
+        kept_rows = rows[kept_cells]
+        renumbered = torch.full_like(rows, -1)
+        renumbered[kept_cells] = torch.arange(kept_rows.numel(), device=device)
+        self.background_links = renumbered.to(torch.int32).view(links.shape)
+        self.background_data = nn.Parameter(self.background_data.data[kept_rows])
 
     # ---- empty-space skipping
     def accelerate(self):

@@ -28,6 +28,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -122,6 +123,74 @@ class ClockSampler:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
                 "samples": len(sm)}
+
+
+def cpu_model() -> str:
+    """The host CPU's model name (/proc/cpuinfo, else lscpu)."""
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.TimeoutExpired):
+        pass
+    return platform.processor() or platform.machine()
+
+
+def reference_grid(svox2, g, device, opt_kw=None):
+    """The reference's own SparseGrid (oracle/_ref/src, its unmodified package) holding the
+    synthetic tables of g: links, density and SH replace the constructor's tables."""
+    grid = svox2.SparseGrid(reso=2, basis_dim=9, device=device)
+    grid.links = g.links.to(device)
+    grid.density_data = torch.nn.Parameter(g.density.to(device))
+    grid.sh_data = torch.nn.Parameter(g.sh.to(device))
+    grid.capacity = int(g.density.shape[0])
+    grid.opt.step_size = 0.5
+    grid.opt.sigma_thresh = 1e-8
+    grid.opt.stop_thresh = 1e-7
+    grid.opt.background_brightness = 1.0
+    for k, v in (opt_kw or {}).items():
+        setattr(grid.opt, k, v)
+    return grid
+
+
+def reference_cpu_step(svox2, grid, o, d, gt) -> float:
+    """One step of the reference's own pure-PyTorch path: volume_render(use_kernel=False) and the
+    MSE loss's autograd backward (svox2/svox2.py:658-884).  Returns seconds."""
+    for p in (grid.density_data, grid.sh_data):
+        p.grad = None
+    t0 = time.perf_counter()
+    rgb = grid.volume_render(svox2.Rays(o, d), use_kernel=False)
+    torch.nn.functional.mse_loss(rgb, gt).backward()
+    return time.perf_counter() - t0
+
+
+def reference_cpu_64(budget_runs: int = 3):
+    """The reference's own CPU path on the 64^3 dense configuration in full (4096 rays, seed 0):
+    median of budget_runs steps after one warm-up, or None when its package is not staged."""
+    from oracle import ref_cuda
+    from svox2_gb300 import synthetic as S
+
+    svox2 = ref_cuda.import_reference_package(with_extension=False)
+    if svox2 is None:
+        return None
+    g = S.make_grid(64, occupancy=None, seed=0)
+    grid = reference_grid(svox2, g, "cpu")
+    o, d, gt = S.make_rays(4096, seed=0)
+    reference_cpu_step(svox2, grid, o, d, gt)
+    times = [reference_cpu_step(svox2, grid, o, d, gt) for _ in range(budget_runs)]
+    t = statistics.median(times)
+    return {"value": 4096 / t, "unit": "rays/s", "threads": torch.get_num_threads(),
+            "sample": "the reference's own volume_render(use_kernel=False) + MSE backward (its unmodified "
+                      "package), 64^3 dense SH9 FP32, 4096 rays in full, median of "
+                      f"{budget_runs} after a warm-up: {t:.2f} s per step"}
 
 
 def max_over_ranks(ms: float, dist, device) -> float:
@@ -618,6 +687,101 @@ def run_serve(args):
     print(json.dumps(line), flush=True)
 
 
+def run_refgpu(args):
+    """The reference's own CUDA training step on the 256^3 training workload, beside this
+    library's, on the same GPU in the same process: its unmodified package (oracle/_ref/src) on
+    its own compiled extension (oracle/_ref), SparseGrid.volume_render_fused + inplace_tv_grad +
+    inplace_tv_color_grad + optim_density_step + optim_sh_step, 1M rays per step, CUDA events.
+    The plain-FP32 GPU form that this library's kernels replace."""
+    from oracle import ref_cuda
+
+    svox2 = ref_cuda.import_reference_package(with_extension=True)
+    if svox2 is None or svox2.svox2._C is None:
+        print(json.dumps({"config": "refgpu", "unavailable": "the reference's extension is not built here"}))
+        return
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    steps, warm = min(args.steps, 10), max(args.warmup, 3)
+    g, grid, batches = build_workload(dev, seed_rays=1000, n_batches=4)
+    dev_batches = [tuple(t.to(dev) for t in b) for b in batches]
+    rgrid = reference_grid(svox2, g, dev)
+
+    def ref_step(o, d, gt, fused_ev=None):
+        if fused_ev is not None:
+            fused_ev[0].record()
+        rgb = rgrid.volume_render_fused(svox2.Rays(o, d), gt)
+        if fused_ev is not None:
+            fused_ev[1].record()
+        rgrid.inplace_tv_grad(rgrid.density_data.grad, scaling=1e-5, sparse_frac=0.01, contiguous=True)
+        rgrid.inplace_tv_color_grad(rgrid.sh_data.grad, scaling=1e-3, sparse_frac=0.01, contiguous=True)
+        rgrid.optim_density_step(30.0, beta=0.95, epsilon=1e-8)
+        rgrid.optim_sh_step(1e-2, beta=0.95, epsilon=1e-8)
+        return rgb
+
+    def timed(step_fn, fused_evs):
+        for i in range(warm):
+            step_fn(*dev_batches[i % 4])
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for i in range(steps):
+            step_fn(*dev_batches[i % 4], fused_evs[i])
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / steps, sum(x.elapsed_time(y) for x, y in fused_evs) / steps
+
+    mk = lambda: [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    with ClockSampler(0) as clk_ref:
+        ref_ms, ref_fused_ms = timed(ref_step, mk())
+
+    def our_step(o, d, gt, ev=None):
+        return train_step(grid, o, d, gt, ev=ev)
+
+    with ClockSampler(0) as clk_ours:
+        our_ms, our_fused_ms = timed(our_step, mk())
+    line = {"config": "refgpu", "workload": WORKLOAD, "rays_per_step": Q, "steps": steps, "warmup": warm,
+            "reference": {"ms_per_step": ref_ms, "rays_per_s": Q / ref_ms * 1e3, "fused_render_ms": ref_fused_ms,
+                          "what": "sxyu/svox2's own SparseGrid training step on its own CUDA extension, "
+                                  "built unmodified for sm_103a", "clocks": clk_ref.summary()},
+            "ours": {"ms_per_step": our_ms, "rays_per_s": Q / our_ms * 1e3, "fused_render_ms": our_fused_ms,
+                     "clocks": clk_ours.summary()},
+            "speedup_step": ref_ms / our_ms, "speedup_fused_render": ref_fused_ms / our_fused_ms}
+    print(json.dumps(line), flush=True)
+
+
+def run_refcpu(args):
+    """The reference's own pure-PyTorch path (volume_render(use_kernel=False) + MSE backward,
+    its unmodified package) on the host cores: the 64^3 dense configuration in full, and the
+    256^3 training workload at the ray counts of --refcpu-rays, with a fit t = a + b Q and the
+    1M-ray step it extrapolates to."""
+    from oracle import ref_cuda
+    from svox2_gb300 import synthetic as S
+
+    svox2 = ref_cuda.import_reference_package(with_extension=False)
+    if svox2 is None:
+        print(json.dumps({"config": "refcpu", "unavailable": "the reference's package is not staged here"}))
+        return
+    out = {"config": "refcpu", "cpu_model": cpu_model(), "torch_threads": torch.get_num_threads(),
+           "cores": os.cpu_count(), "dense64": reference_cpu_64(3)}
+    g = S.make_grid(RESO, occupancy=OCC, n_balls=N_BALLS, seed=0)
+    grid = reference_grid(svox2, g, "cpu")
+    pts = []
+    for q in [int(x) for x in args.refcpu_rays.split(",")]:
+        o, d, gt = S.make_rays(q, seed=12345)
+        t = reference_cpu_step(svox2, grid, o, d, gt)
+        pts.append((q, t))
+        print(json.dumps({"refcpu_point": {"rays": q, "seconds": t}}), flush=True)
+    (q0, t0), (q1, t1) = pts[0], pts[-1]
+    b = (t1 - t0) / (q1 - q0) if q1 != q0 else 0.0
+    a = t0 - b * q0
+    out["train256"] = {"points": [{"rays": q, "seconds": t, "rays_per_s": q / t} for q, t in pts],
+                       "fit": {"a_s": a, "b_s_per_ray": b},
+                       "extrapolated_1M_ray_step_s": a + b * 1_000_000,
+                       "extrapolated_rays_per_s": 1_000_000 / (a + b * 1_000_000),
+                       "note": "extrapolated from the fit, not measured"}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     global Q
     ap = argparse.ArgumentParser()
@@ -628,11 +792,15 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--rays", type=int, default=1_000_000, help="rays per step (profiling runs use a smaller case)")
     ap.add_argument("--skip-e2e", action="store_true", help="leave out the host-copy arm (profiling runs)")
-    ap.add_argument("--config", default="train", choices=["train", "mixed", "serve", "render", "background"],
+    ap.add_argument("--config", default="train",
+                    choices=["train", "mixed", "serve", "render", "background", "refgpu", "refcpu"],
                     help="train: the 256^3 training step (default); mixed: 512^3 BF16/FP16 SH vs FP32; "
                          "serve: continuous-batching server vs serial launches; "
                          "render: forward-only render of the 256^3 workload, FP32 and BF16 SH; "
-                         "background: the training step with the T&T MSI background")
+                         "background: the training step with the T&T MSI background; "
+                         "refgpu: the reference's own CUDA training step beside this library's; "
+                         "refcpu: the reference's own CPU path (64^3 in full, 256^3 ray subsets + fit)")
+    ap.add_argument("--refcpu-rays", default="256,1024", help="refcpu: ray counts of the 256^3 subsets")
     ap.add_argument("--requests", type=int, default=600, help="serve: number of requests in the stream")
     ap.add_argument("--bg-layers", type=int, default=64, help="background: MSI layers (the T&T configuration's 64)")
     ap.add_argument("--bg-reso", type=int, default=1024, help="background: MSI resolution (T&T: 1024)")
@@ -649,6 +817,12 @@ def main():
         return
     if args.config == "background":
         run_background(args)
+        return
+    if args.config == "refgpu":
+        run_refgpu(args)
+        return
+    if args.config == "refcpu":
+        run_refcpu(args)
         return
     Q = args.rays
     args.warmup = max(args.warmup, 3)
@@ -781,7 +955,11 @@ def emit(args, rank, world, g, value, e2e_val, total_ms, kern_ms, n_eval, clk):
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         rate, cores, desc = cpu_sample(g)
-        cpu = {"value": rate, "unit": "rays/s", "cores": cores, "kind": "port", "sample": desc}
+        cpu = {"value": rate, "unit": "rays/s", "cores": cores, "kind": "port", "sample": desc,
+               "cpu_model": cpu_model(), "torch_threads": torch.get_num_threads()}
+        ref_cpu = reference_cpu_64()
+        if ref_cpu is not None:
+            cpu["reference_cpu_path"] = ref_cpu
 
     if rank == 0:
         line = {

@@ -25,6 +25,12 @@
  * float run (oracle_render's stop_in), so that it also stops where the float
  * run stopped.
  *
+ * A sample's opacity 1 - exp(-x) is OMX(-x): the float instance subtracts, as
+ * the reference does (for x below 2^-24 that is exactly 0), the double
+ * instance uses -expm1(-x), the same quantity without the cancellation, so the
+ * yardstick is exact to double precision for the thin media where the
+ * subtraction is not.
+ *
  * Two places where the reference's device code calls approximate hardware
  * functions are restated from their mathematical definition:
  *   - rnorm3df (svox2/csrc/include/cuda_util.cuh:87-92) -> 1/sqrt formed in double;
@@ -306,7 +312,7 @@ static void FN(fwd_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const f
       REAL col[3];
       FN(sample_colour)(g, &s, basis, col);
       const REAL pcnt = (REAL)ws * sigma;
-      const REAL w = EXP(lt) * ((REAL)1 - EXP(-pcnt));
+      const REAL w = EXP(lt) * OMX(-pcnt);
       lt = lt - pcnt;
       ++*n_eval;
       ++ne;
@@ -330,12 +336,15 @@ static void FN(fwd_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const f
  * accum left after the last sample (beta term taken out) and the log transmittance there,
  * which the MSI background's backward starts from (cuvol.cu:253-258, 374-383).
  * mag_density / mag_sh (optional) receive, per gradient entry, the scale against which
- * float arithmetic loses precision: the sum over its terms of |term| * F, the density term
- * counting its two parts |tc T_after| and the ray's total light A = sum_c |gout_c colour_c|
- * + |beta term| (an upper bound on |accum|) separately.  F = 1 + sum of |log T| over the
- * ray's samples so far bounds, in units of the float rounding unit, the rounding error that
- * the float chain of log T subtractions has built up by then: every later weight and
- * transmittance inherits it as a relative error. */
+ * float arithmetic loses precision: the sum over its terms of |term| * F.  F = 1 + sum of
+ * |log T| over the ray's samples so far bounds, in units of the float rounding unit, the
+ * rounding error that the float chain of log T subtractions has built up by then: every
+ * later weight and transmittance inherits it as a relative error.  The density term counts
+ * its two parts separately: |tc T_after| * F, and the light behind the sample, bounded by
+ * the ray's total light A = sum_c |gout_c colour_c| + |beta term|, with F + nmax (a sum of
+ * up to nmax terms, the ray's most samples, in any order).  An SH term whose colour channel
+ * sits on the clamp (|colour + 0.5| <= 1e-5, within float reach of the kink) may be in or
+ * out of the float sum: it counts 2^24 times, i.e. its whole size. */
 static void FN(bwd_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const float org[3], const float dir[3],
                         const REAL color[3], REAL log_t_in, const REAL gout[3], REAL beta_loss, REAL sparsity,
                         REAL* grad_density, REAL* grad_sh, uint8_t* mask, REAL* accum_out, REAL* log_t_out,
@@ -345,12 +354,14 @@ static void FN(bwd_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const f
   const int64_t co[8] = {0, 1, offy, offy + 1, offx, offx + 1, offx + offy, offx + offy + 1};
   const REAL log_stop = FN(log_stop)(opt->stop_thresh);
   const float step = opt->step;
-  REAL basis[9], dr[3] = {dir[0], dir[1], dir[2]}, lt = 0, accum, beta_term = 0, amag, fchain = 1;
+  REAL basis[9], dr[3] = {dir[0], dir[1], dir[2]}, lt = 0, accum, beta_term = 0, amag, fchain = 1, nmax;
   float t, ws;
   FN(ray_t) r;
   int c, j, ne = 0;
   FN(calc_sh)(bd, dr, basis);
   FN(find_bounds)(&r, org, dir, g, opt);
+  /* the most samples the ray can take: the length of any sum over them */
+  nmax = r.tmax >= r.tmin ? ((REAL)r.tmax - (REAL)r.tmin) / (REAL)step + (REAL)2 : (REAL)0;
   accum = FMA(color[0], gout[0], FMA(color[1], gout[1], color[2] * gout[2]));
   *accum_out = accum;
   *log_t_out = 0;
@@ -377,15 +388,17 @@ static void FN(bwd_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const f
     if (opt->last_opaque && t + step > r.tmax) ws = 1e9f;
     if (sigma > (REAL)opt->sigma_thresh) {
       REAL col[3], tot[3], in01[3], wts[8], gsp = 0;
+      int kink[3];
       FN(sample_colour)(g, &s, basis, col);
       const REAL pcnt = (REAL)ws * sigma;
-      const REAL w = EXP(lt) * ((REAL)1 - EXP(-pcnt));
+      const REAL w = EXP(lt) * OMX(-pcnt);
       lt = lt - pcnt;
       ++ne;
       for (c = 0; c < 3; ++c) {
         const REAL lc = col[c] + (REAL)0.5;
         const REAL tc = FMAX(lc, (REAL)0);
         in01[c] = (tc == lc) ? (REAL)1 : (REAL)0;
+        kink[c] = FABS(lc) <= (REAL)1e-5;
         tot[c] = tc * gout[c];
       }
       const REAL tcs = (tot[0] + tot[2]) + tot[1];
@@ -422,10 +435,12 @@ static void FN(bwd_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const f
         if (mag_sh)
           for (c = 0; c < C; ++c)
             FN(atomic_add)(mag_sh + (int64_t)lk * C + c,
-                           fchain * FABS(wts[j] * (basis[c % bd] * (w * in01[c / bd] * gout[c / bd]))));
+                           (kink[c / bd] ? (REAL)16777216 : fchain * in01[c / bd]) *
+                               FABS(wts[j] * (basis[c % bd] * (w * gout[c / bd]))));
         if (mag_density)
           FN(atomic_add)(mag_density + lk,
-                         fchain * wts[j] * ((REAL)ws * (FABS(tcs * tn) + amag) + FABS(gsp)));
+                         wts[j] * ((REAL)ws * (fchain * FABS(tcs * tn) + (fchain + nmax) * amag) +
+                                   fchain * FABS(gsp)));
         if (mask) mask[lk] = 1;
       }
       if (FN(stops)(stop_in, lt, log_stop, ne)) break;
@@ -575,7 +590,7 @@ static void FN(bg_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const RE
     width = cpu ? t - t_last : invr_last - invr;
     if (sigma > 0) {
       const REAL pcnt = cpu ? b.ws * sigma * width : width * b.ws * sigma;
-      const REAL w = EXP(lt) * ((REAL)1 - EXP(-pcnt));
+      const REAL w = EXP(lt) * OMX(-pcnt);
       lt = lt - pcnt;
       if (n_samples) ++*n_samples;
       if (gout == NULL) {
@@ -735,7 +750,7 @@ static REAL FN(depth_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const
         if (sigma > (REAL)sigma_thresh) return ((REAL)t / step) * (REAL)r.world_step;
       } else if (sigma > (REAL)opt->sigma_thresh) {
         const REAL pcnt = (REAL)r.world_step * sigma;
-        const REAL w = EXP(lt) * ((REAL)1 - EXP(-pcnt));
+        const REAL w = EXP(lt) * OMX(-pcnt);
         lt = lt - pcnt;
         outv = outv + w * ((REAL)t / step) * (REAL)r.world_step;
         if (lt < log_stop) break;
@@ -823,7 +838,7 @@ void FN(oracle_grid_weight_render)(const float* data, const int size[3], const o
       }
       if (sigma > (REAL)1e-8f) {
         const REAL la = -((REAL)r.world_step * sigma);
-        const REAL w = EXP(ll) * ((REAL)1 - EXP(la));
+        const REAL w = EXP(ll) * OMX(la);
         ll = ll + la;
         for (j = 0; j < 8; ++j)
           if (w > wmax[idx + co[j]]) wmax[idx + co[j]] = w;

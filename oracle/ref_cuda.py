@@ -167,6 +167,38 @@ def load():
     return mod
 
 
+def import_reference_package(with_extension: bool = True):
+    """The reference's own Python package (sxyu/svox2 ``svox2``, staged unmodified into
+    oracle/_ref/src), bound to its own compiled extension when with_extension and the extension
+    is built for this machine; otherwise it runs its pure-PyTorch path only (its ``_C`` is None).
+    The package imports tqdm (a progress bar) at module level; where tqdm is not installed a
+    pass-through stand-in is registered under that name.  Returns None when nothing is staged."""
+    if not (SRC_DIR / "svox2" / "svox2.py").exists():
+        return None
+    if "svox2" in sys.modules:
+        return sys.modules["svox2"]
+    try:
+        import tqdm  # noqa: F401
+    except ImportError:
+        import types
+
+        stub = types.ModuleType("tqdm")
+        stub.tqdm = lambda it=None, *a, **k: it
+        sys.modules["tqdm"] = stub
+    if with_extension:
+        mod = load()
+        if mod is not None:
+            sys.modules["svox2.csrc"] = mod
+    if str(SRC_DIR) not in sys.path:
+        sys.path.insert(0, str(SRC_DIR))
+    import warnings
+
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        import svox2
+    return svox2
+
+
 if __name__ == "__main__":
     root = Path(sys.argv[1]) if len(sys.argv) > 1 else DEFAULT_REF_ROOT
     print("staged:", stage(root) or staged())

@@ -47,6 +47,7 @@ typedef struct {
 #define ASIN asinf
 #define ATAN2 atan2f
 #define FABS fabsf
+#define OMX(y) (1.f - expf(y))
 #include "oracle_impl.h"
 #undef REAL
 #undef SUFFIX
@@ -60,6 +61,7 @@ typedef struct {
 #undef ASIN
 #undef ATAN2
 #undef FABS
+#undef OMX
 
 #define REAL double
 #define SUFFIX _f64
@@ -73,6 +75,7 @@ typedef struct {
 #define ASIN asin
 #define ATAN2 atan2
 #define FABS fabs
+#define OMX(y) (-expm1(y))
 #include "oracle_impl.h"
 
 /* accel_dist_prop, svox2/csrc/misc_kernel.cu:108-181 (kernels) and 356-416 (host):

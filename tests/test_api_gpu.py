@@ -10,7 +10,7 @@ from oracle import oracle as O
 from svox2_gb300 import Camera, Rays, SparseGrid
 from svox2_gb300 import synthetic as S
 
-from helpers import assert_grad, assert_rgb
+from helpers import assert_grad, assert_grad_f64, assert_rgb
 
 pytestmark = pytest.mark.gpu
 
@@ -59,10 +59,14 @@ def test_autograd_render_matches_fused(z_order):
     assert torch.allclose(rgb, rgb2, rtol=0, atol=0)
     assert_grad(g_d.cpu().numpy(), grid.density_data.grad.cpu().numpy(), "density grad autograd vs fused")
     assert_grad(g_s.cpu().numpy(), grid.sh_data.grad.cpu().numpy(), "sh grad autograd vs fused")
-    ref = O.render(_oracle_grid(grid), O.Opt(1.0, 0.5, 1e-8, 1e-7), o.numpy(), d.numpy(), mode=1,
-                   rgb_gt=gt.numpy())
+    og = _oracle_grid(grid)
+    ref = O.render(og, O.Opt(1.0, 0.5, 1e-8, 1e-7), o.numpy(), d.numpy(), mode=1, rgb_gt=gt.numpy())
+    r64 = O.render(og, O.Opt(1.0, 0.5, 1e-8, 1e-7), o.numpy(), d.numpy(), mode=1, rgb_gt=gt.numpy(), prec="f64",
+                   stops=ref["stops"], want_magnitude=True)
     assert_rgb(rgb.detach().cpu().numpy(), ref["rgb"])
-    assert_grad(grid.sh_data.grad.cpu().numpy(), ref["grad_sh"])
+    assert_grad_f64(grid.sh_data.grad.cpu().numpy(), r64["grad_sh"], r64["mag_sh"], "api grad_sh")
+    assert_grad_f64(grid.density_data.grad.cpu().numpy(), r64["grad_density"], r64["mag_density"],
+                    "api grad_density")
     np.testing.assert_array_equal(grid.sparse_grad_indexer.cpu().numpy(), ref["mask"])
 
 

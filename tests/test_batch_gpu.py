@@ -16,7 +16,7 @@ from svox2_gb300 import _lib
 from svox2_gb300 import csrc
 from svox2_gb300 import synthetic as S
 
-from helpers import assert_grad, assert_rgb, grid_pair, opt_struct
+from helpers import assert_grad, assert_grad_f64, assert_rgb, grid_pair, opt_struct
 
 pytestmark = pytest.mark.gpu
 
@@ -108,9 +108,12 @@ def test_batch_fused_matches_oracle_per_grid(sh_dtype, use_order):
     rgbs, bufs = _batch(1, grids, rays, opt, sh_dtype, use_order, accum_for=(1,))
     for (spec, og), (o, d, gt), rgb, b in zip(grids, rays, rgbs, bufs):
         ref = O.render(og, oopt, o.numpy(), d.numpy(), mode=1, rgb_gt=gt.numpy(), prec="f32")
+        r64 = O.render(og, oopt, o.numpy(), d.numpy(), mode=1, rgb_gt=gt.numpy(), prec="f64", stops=ref["stops"],
+                       want_magnitude=True)
         assert_rgb(rgb, ref["rgb"], "rgb")
-        assert_grad(b["gd"].cpu().numpy(), ref["grad_density"], "grad_density")
-        assert_grad(b["gs"].cpu().numpy(), ref["grad_sh"], "grad_sh")
+        assert_rgb(rgb, r64["rgb"], "rgb vs float64")
+        assert_grad_f64(b["gd"].cpu().numpy(), r64["grad_density"], r64["mag_density"], "batch grad_density")
+        assert_grad_f64(b["gs"].cpu().numpy(), r64["grad_sh"], r64["mag_sh"], "batch grad_sh")
         np.testing.assert_array_equal(b["mask"].cpu().numpy(), ref["mask"])
 
 

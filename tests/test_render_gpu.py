@@ -17,7 +17,7 @@ import torch
 from oracle import oracle as O
 from svox2_gb300 import synthetic as S
 
-from helpers import assert_grad_f64, check_fused, grid_pair, opt_struct, rays_pair, stats_dict as _stats
+from helpers import assert_grad_f64, assert_rgb, check_fused, grid_pair, opt_struct, rays_pair, stats_dict as _stats
 
 pytestmark = pytest.mark.gpu
 

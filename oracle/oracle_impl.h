@@ -252,6 +252,20 @@ static REAL FN(trilerp)(const oracle_grid_t* g, const FN(sample_t) * s, const fl
   return FN(lerp)(ix0, ix1, p0);
 }
 
+/* Largest |value| of channel idx over the 8 corners of the sample's cell: the scale of the
+ * absolute rounding error of its trilinear interpolation. */
+static REAL FN(corner_max)(const oracle_grid_t* g, const FN(sample_t) * s, const float* data, int stride, int idx) {
+  const int64_t offy = g->size[2], offx = (int64_t)g->size[1] * g->size[2];
+  const int64_t co[8] = {0, 1, offy, offy + 1, offx, offx + 1, offx + offy, offx + offy + 1};
+  REAL m = 0;
+  int j;
+  for (j = 0; j < 8; ++j) {
+    int32_t lk = s->lp[co[j]];
+    if (lk >= 0) m = FMAX(m, FABS((REAL)data[(int64_t)lk * stride + idx]));
+  }
+  return m;
+}
+
 /* Colour sum per channel group, before the +0.5 offset. */
 static void FN(sample_colour)(const oracle_grid_t* g, const FN(sample_t) * s, const REAL basis[9], REAL col[3]) {
   const int bd = g->basis_dim, C = 3 * bd;
@@ -273,7 +287,8 @@ static int FN(stops)(int stop_in, REAL lt, REAL log_stop, int n_done) {
  * the log transmittance the reference reports (-1e3 after an early stop).
  * *stop_out: the ray's evaluated-sample count at its early stop, or -1. */
 static void FN(fwd_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const float org[3], const float dir[3],
-                        REAL out[3], REAL* log_t, uint64_t* trace, uint64_t* n_eval, int stop_in, int* stop_out) {
+                        REAL out[3], REAL* log_t, uint64_t* trace, uint64_t* n_eval, int stop_in, int* stop_out,
+                        REAL* chain_out) {
   const REAL log_stop = FN(log_stop)(opt->stop_thresh);
   const float step = opt->step;
   REAL basis[9], dr[3] = {dir[0], dir[1], dir[2]}, outv[3] = {0, 0, 0}, lt = 0;
@@ -281,7 +296,9 @@ static void FN(fwd_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const f
   FN(ray_t) r;
   uint64_t h = 1469598103934665603ull;
   int c, ne = 0;
+  REAL chain = 1;
   if (stop_out) *stop_out = -1;
+  if (chain_out) *chain_out = 1;
   FN(calc_sh)(g->basis_dim, dr, basis);
   FN(find_bounds)(&r, org, dir, g, opt);
   if (r.tmin > r.tmax) {
@@ -314,6 +331,7 @@ static void FN(fwd_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const f
       const REAL pcnt = (REAL)ws * sigma;
       const REAL w = EXP(lt) * OMX(-pcnt);
       lt = lt - pcnt;
+      chain += FABS(lt);
       ++*n_eval;
       ++ne;
       for (c = 0; c < 3; ++c) outv[c] = outv[c] + w * FMAX(col[c] + (REAL)0.5, (REAL)0);
@@ -329,6 +347,7 @@ static void FN(fwd_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const f
   for (c = 0; c < 3; ++c) out[c] = g->bg_nlayers == 0 ? outv[c] + EXP(lt) * (REAL)opt->bg : outv[c];
   *log_t = lt;
   if (trace) *trace = h;
+  if (chain_out) *chain_out = chain;
 }
 
 /* trace_ray_cuvol_backward, render_lerp_kernel_cuvol.cu:227-383, forward order:
@@ -342,19 +361,28 @@ static void FN(fwd_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const f
  * later weight and transmittance inherits it as a relative error.  The density term counts
  * its two parts separately: |tc T_after| * F, and the light behind the sample, bounded by
  * the ray's total light A = sum_c |gout_c colour_c| + |beta term|, with F + nmax (a sum of
- * up to nmax terms, the ray's most samples, in any order).  An SH term whose colour channel
- * sits on the clamp (|colour + 0.5| <= 1e-5, within float reach of the kink) may be in or
- * out of the float sum: it counts 2^24 times, i.e. its whole size. */
+ * up to nmax terms, the ray's most samples, in any order).  An SH term basis_k * X counts
+ * |X| (Fw |basis_k| + e_k), with Fw = F + 4 max|corner density| / sigma: the float
+ * trilinear interpolation lerp(a, b, w) = a + w (b - a) errs by a few rounding units of its
+ * corner values, which is large against a small sigma (a sample just inside a face whose far
+ * corners are empty), and the sample's weight inherits it; gerr_c (from oracle_render: the
+ * relative error, in rounding units, of a float run's loss residual out - gt, large where the
+ * colour nearly matches its target) multiplies every term of channel c; the float basis of k = 6 (C * (2 zz - xx - yy)) and k = 8
+ * (C * (xx - yy)) is a difference of float squares of a unit direction, whose absolute
+ * error is e_k = 2 |C| rounding units however small the difference; the other basis
+ * functions are products, relative to their value.  An SH term whose colour channel sits on
+ * the clamp (|colour + 0.5| <= 1e-5, within float reach of the kink) may be in or out of the
+ * float sum: it counts 2^24 times, i.e. its whole size. */
 static void FN(bwd_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const float org[3], const float dir[3],
                         const REAL color[3], REAL log_t_in, const REAL gout[3], REAL beta_loss, REAL sparsity,
                         REAL* grad_density, REAL* grad_sh, uint8_t* mask, REAL* accum_out, REAL* log_t_out,
-                        int stop_in, REAL* mag_density, REAL* mag_sh) {
+                        int stop_in, REAL* mag_density, REAL* mag_sh, const REAL gerr[3]) {
   const int bd = g->basis_dim, C = 3 * bd;
   const int64_t offy = g->size[2], offx = (int64_t)g->size[1] * g->size[2];
   const int64_t co[8] = {0, 1, offy, offy + 1, offx, offx + 1, offx + offy, offx + offy + 1};
   const REAL log_stop = FN(log_stop)(opt->stop_thresh);
   const float step = opt->step;
-  REAL basis[9], dr[3] = {dir[0], dir[1], dir[2]}, lt = 0, accum, beta_term = 0, amag, fchain = 1, nmax;
+  REAL basis[9], berr[9], dr[3] = {dir[0], dir[1], dir[2]}, lt = 0, accum, beta_term = 0, amag, fchain = 1, nmax;
   float t, ws;
   FN(ray_t) r;
   int c, j, ne = 0;
@@ -362,6 +390,11 @@ static void FN(bwd_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const f
   FN(find_bounds)(&r, org, dir, g, opt);
   /* the most samples the ray can take: the length of any sum over them */
   nmax = r.tmax >= r.tmin ? ((REAL)r.tmax - (REAL)r.tmin) / (REAL)step + (REAL)2 : (REAL)0;
+  for (c = 0; c < 9; ++c) berr[c] = 0;
+  if (bd >= 9) {
+    berr[6] = (REAL)2 * (REAL)0.31539156525252005;
+    berr[8] = (REAL)2 * (REAL)0.5462742152960396;
+  }
   accum = FMA(color[0], gout[0], FMA(color[1], gout[1], color[2] * gout[2]));
   *accum_out = accum;
   *log_t_out = 0;
@@ -404,6 +437,7 @@ static void FN(bwd_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const f
       const REAL tcs = (tot[0] + tot[2]) + tot[1];
       const REAL tn = EXP(lt);
       fchain += FABS(lt);
+      const REAL fw = fchain + (REAL)4 * FN(corner_max)(g, &s, g->density, 1, 0) / sigma;
       accum = accum - w * tcs;
       REAL gsig = (REAL)ws * (tcs * tn - accum);
       if (sparsity > 0) {
@@ -435,8 +469,10 @@ static void FN(bwd_ray)(const oracle_grid_t* g, const oracle_opt_t* opt, const f
         if (mag_sh)
           for (c = 0; c < C; ++c)
             FN(atomic_add)(mag_sh + (int64_t)lk * C + c,
-                           (kink[c / bd] ? (REAL)16777216 : fchain * in01[c / bd]) *
-                               FABS(wts[j] * (basis[c % bd] * (w * gout[c / bd]))));
+                           FABS(wts[j] * (w * gout[c / bd])) *
+                               (kink[c / bd] ? (REAL)16777216 * FABS(basis[c % bd])
+                                             : in01[c / bd] * ((fw + gerr[c / bd]) * FABS(basis[c % bd]) +
+                                                                   berr[c % bd])));
         if (mag_density)
           FN(atomic_add)(mag_density + lk,
                          wts[j] * ((REAL)ws * (fchain * FABS(tcs * tn) + (fchain + nmax) * amag) +
@@ -678,7 +714,7 @@ void FN(oracle_render)(const oracle_grid_t* g, const oracle_opt_t* opt, const fl
 #pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads) reduction(+ : total, total_bg)
   for (q = 0; q < Q; ++q) {
     float org[3], dir[3];
-    REAL orgr[3], dirr[3], out[3], gout[3], lt = 0, acc_b = 0, lt_b = 0;
+    REAL orgr[3], dirr[3], out[3], gout[3], gerr[3] = {0, 0, 0}, lt = 0, acc_b = 0, lt_b = 0, chain = 1;
     const int bg = g->bg_nlayers > 0;
     const int sin_ = stop_in ? stop_in[q] : -2;
     uint64_t ne = 0, nb = 0;
@@ -690,16 +726,22 @@ void FN(oracle_render)(const oracle_grid_t* g, const oracle_opt_t* opt, const fl
       dirr[i] = (REAL)dir[i];
     }
     if (mode == 0 || mode == 1) {
-      FN(fwd_ray)(g, opt, org, dir, out, &lt, trace ? trace + q : NULL, &ne, sin_, &so);
+      FN(fwd_ray)(g, opt, org, dir, out, &lt, trace ? trace + q : NULL, &ne, sin_, &so, &chain);
       /* render_background_kernel skips rays whose log transmittance is below -25 */
       if (bg && lt >= (REAL)-25) FN(bg_ray)(g, opt, orgr, dirr, lt, NULL, 0, 0, out, NULL, NULL, &nb);
       for (i = 0; i < 3; ++i) rgb_out[q * 3 + i] = out[i];
       if (stop_out) stop_out[q] = so;
     }
     if (mode == 1) {
-      for (i = 0; i < 3; ++i) gout[i] = (out[i] - (REAL)rgb_gt[q * 3 + i]) * norm;
+      for (i = 0; i < 3; ++i) {
+        const REAL res = out[i] - (REAL)rgb_gt[q * 3 + i];
+        gout[i] = res * norm;
+        /* the residual's relative error in a float run, in rounding units: the colour's
+         * (chain + 16) units of |out|, over |out - gt| */
+        gerr[i] = (chain + (REAL)16) * FABS(out[i]) / FMAX(FABS(res), (REAL)1e-30);
+      }
       FN(bwd_ray)(g, opt, org, dir, out, lt, gout, (REAL)beta_loss / (REAL)Q, (REAL)sparsity, grad_density,
-                  grad_sh, mask, &acc_b, &lt_b, sin_, mag_density, mag_sh);
+                  grad_sh, mask, &acc_b, &lt_b, sin_, mag_density, mag_sh, gerr);
       /* the fused path's background backward starts from the forward's log transmittance */
       if (bg && lt >= (REAL)-25)
         FN(bg_ray)(g, opt, orgr, dirr, lt, gout, acc_b, (REAL)sparsity, NULL, grad_bg, mask_bg, NULL);
@@ -709,7 +751,7 @@ void FN(oracle_render)(const oracle_grid_t* g, const oracle_opt_t* opt, const fl
         gout[i] = (REAL)grad_out[q * 3 + i];
       }
       FN(bwd_ray)(g, opt, org, dir, out, 0, gout, 0, 0, grad_density, grad_sh, NULL, &acc_b, &lt_b, sin_,
-                  mag_density, mag_sh);
+                  mag_density, mag_sh, gerr);
       /* volume_render_cuvol_backward: from the backward pass's own log transmittance */
       if (bg && lt_b >= (REAL)-25)
         FN(bg_ray)(g, opt, orgr, dirr, lt_b, gout, acc_b, 0, NULL, grad_bg, NULL, NULL);
@@ -861,7 +903,7 @@ void FN(oracle_render_image)(const oracle_grid_t* g, const oracle_opt_t* opt, co
     uint64_t ne = 0;
     int i;
     FN(camera_ray)((int)(q % cam->width), (int)(q / cam->width), cam, dir, org);
-    FN(fwd_ray)(g, opt, org, dir, rgb, &lt, trace ? trace + q : NULL, &ne, -2, NULL);
+    FN(fwd_ray)(g, opt, org, dir, rgb, &lt, trace ? trace + q : NULL, &ne, -2, NULL, NULL);
     for (i = 0; i < 3; ++i) {
       orgr[i] = (REAL)org[i];
       dirr[i] = (REAL)dir[i];

@@ -409,8 +409,11 @@ const char* svx_last_error(void);
 /* SVX_ABI_VERSION of the loaded library. */
 int svx_abi_version(void);
 
-/* Largest number of evaluated samples per ray whose colours the fused
- * adjoint keeps on chip; samples past it are re-gathered in the reverse pass. */
+/* Largest number of evaluated samples per ray whose colours the adjoint keeps
+ * in shared memory when it has no global colour cache (the allocation-free
+ * render and the batch launch); samples past it are re-gathered in the
+ * reverse pass.  The fused and backward renders keep a global cache as long
+ * as the grid's longest ray (up to 4096 samples). */
 int svx_color_cache_capacity(void);
 
 #ifdef __cplusplus

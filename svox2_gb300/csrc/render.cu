@@ -416,14 +416,15 @@ static int render_rays(const svx_grid_t* grid, const svx_rays_t* rays, const svx
   rc = make_opt(opt, &o);
   if (rc) return rc;
   const GridP g = make_grid(grid);
+  double max_samples = 0.0;
   if (MODE != kFwd) {
     // every ray's samples must fit the adjoint's checkpoints (kNumCkpt x kMaxStride segments)
     const double diag = std::sqrt((double)g.size[0] * g.size[0] + (double)g.size[1] * g.size[1] +
                                   (double)g.size[2] * g.size[2]);
-    const double max_samples = diag / (double)o.step + 2.0;
-    SVX_REQUIRE(max_samples <= (double)kNumCkpt * kMaxStride, SVX_ERR_TOO_LARGE,
+    max_samples = diag / (double)o.step + 2.0;
+    SVX_REQUIRE(max_samples <= (double)kMaxAdjointSamples, SVX_ERR_TOO_LARGE,
                 "up to %.0f samples per ray (grid diagonal / step_size); the adjoint supports %d",
-                max_samples, kNumCkpt * kMaxStride);
+                max_samples, kMaxAdjointSamples);
   }
   io.origins = rays->origins;
   io.dirs = rays->dirs;
@@ -442,6 +443,18 @@ static int render_rays(const svx_grid_t* grid, const svx_rays_t* rays, const svx
   rc = scr.alloc(0, 256);
   if (rc) return rc;
   io.work = reinterpret_cast<unsigned long long*>(scr.p[0]);
+  if (MODE != kFwd) {
+    // The adjoint's colour cache: one slice per resident warp of the launch (the adjoint
+    // instantiations are bounded to kAdjointBlocksPerSm blocks per SM), as long as the grid's
+    // longest ray up to kGlobalCapMax samples.  At the 256^3 workload that is 896 samples, about
+    // 26 MB in all, most of it held in L2 between a ray's forward and reverse passes.
+    const double want = std::ceil(max_samples / 32.0) * 32.0;
+    io.cap = (int)std::min(want, (double)kGlobalCapMax);
+    io.gcol_warps = (long long)num_sms() * kAdjointBlocksPerSm * kWarps;
+    rc = scr.alloc(3, sizeof(float) * 3 * (size_t)io.cap * (size_t)io.gcol_warps);
+    if (rc) return rc;
+    io.gcol = reinterpret_cast<float*>(scr.p[3]);
+  }
   const bool grads = MODE != kFwd && (io.grad_sh != nullptr || io.grad_density != nullptr);
   const int C = grid->sh_data_dim;
   const int stride = (C + 1 + 3) & ~3;
@@ -650,9 +663,9 @@ extern "C" int svx_volume_render_cuvol_fused_noalloc(const svx_grid_t* grid, con
   const double diag = std::sqrt((double)g.size[0] * g.size[0] + (double)g.size[1] * g.size[1] +
                                 (double)g.size[2] * g.size[2]);
   const double max_samples = diag / (double)o.step + 2.0;
-  SVX_REQUIRE(max_samples <= (double)kNumCkpt * kMaxStride, SVX_ERR_TOO_LARGE,
+  SVX_REQUIRE(max_samples <= (double)kMaxAdjointSamples, SVX_ERR_TOO_LARGE,
               "up to %.0f samples per ray (grid diagonal / step_size); the adjoint supports %d", max_samples,
-              kNumCkpt * kMaxStride);
+              kMaxAdjointSamples);
   unsigned long long* scratch = nullptr;
   rc = static_scratch_address(&scratch);
   if (rc) return rc;

@@ -44,7 +44,12 @@ constexpr int kThreads = 128;
 constexpr int kWarps = kThreads / 32;
 constexpr int kNumCkpt = 64;   // stored segment checkpoints per ray before thinning
 constexpr int kMaxStride = 64; // checkpoint thinning limit: 64*64 segments per ray
-constexpr int kDefaultCap = 192;
+// samples per ray the adjoint's checkpoints cover: kNumCkpt checkpoints, each at most kMaxStride
+// segments (of 32 samples) that hold evaluated samples apart
+constexpr int kMaxAdjointSamples = kNumCkpt * kMaxStride * 32;
+constexpr int kDefaultCap = 192;     // shared-memory colour cache (launches without a global one)
+constexpr int kGlobalCapMax = 4096;  // global colour cache: samples per ray, at most
+constexpr int kAdjointBlocksPerSm = 4;  // __launch_bounds__ of the adjoint instantiations
 constexpr long long kSortMinRays = 1 << 15;  // batches below this run in input order
 
 enum Mode { kFwd = 0, kFused = 1, kBwd = 2 };
@@ -104,6 +109,8 @@ struct IoP {
   unsigned long long* eval_count;
   unsigned long long* trace;
   int cap;         // colour cache capacity (samples per ray)
+  float* gcol;     // optional colour cache in global memory: one [cap][3] slice per resident warp
+  long long gcol_warps;  // slices in gcol (warps of the launch)
   // MSI background (grids that have one; render_kernel<..., BG = true>)
   const int32_t* bg_links;     // [2 reso, reso]
   const float* bg_data;        // [bg_cap, bg_nl, 4], rows 16-byte aligned
@@ -1086,13 +1093,22 @@ template <int BD, typename ShT, int MODE, bool IMAGE, bool MULTI, bool BG = fals
 // let four blocks (16 warps) share an SM; the march is latency-bound, so resident warps
 // count for more than the registers a larger budget would save.  The forward-only kernel
 // (no colour cache, no checkpoints: 10 KB per warp) fits five blocks at 102 registers.
-__global__ void __launch_bounds__(kThreads, MODE == kFwd ? 5 : 4) render_kernel(GridP g0, OptP opt, IoP io) {
+__global__ void __launch_bounds__(kThreads, MODE == kFwd ? 5 : kAdjointBlocksPerSm) render_kernel(GridP g0, OptP opt,
+                                                                                               IoP io) {
   constexpr int C = 3 * BD;
   extern __shared__ float4 smem4[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
-  float* wbase = reinterpret_cast<float*>(smem4) + (size_t)wib * warp_smem_floats(C, io.cap, MODE != kFwd);
-  const WarpSmem sm = carve(wbase, C, io.cap, MODE != kFwd);
+  // The adjoint's per-sample colour cache: a slice of io.gcol (global memory, most of it held in
+  // L2 between a ray's forward and reverse passes; sized by the host for the grid's longest ray),
+  // or, without one, cap samples in shared memory.  Samples past the capacity are gathered again.
+  const int scap = io.gcol != nullptr ? 0 : io.cap;
+  float* wbase = reinterpret_cast<float*>(smem4) + (size_t)wib * warp_smem_floats(C, scap, MODE != kFwd);
+  const WarpSmem sm = carve(wbase, C, scap, MODE != kFwd);
+  const long long gslot = (long long)blockIdx.x * kWarps + wib;
+  const bool gown = io.gcol != nullptr && gslot < io.gcol_warps;
+  float* colc = gown ? io.gcol + gslot * io.cap * 3 : sm.col;
+  const int cap = (io.gcol == nullptr || gown) ? io.cap : 0;
   const int grp = lane >> 3, cj = lane & 7;
   const long long n_rays = MULTI ? *io.n_rays_dev : io.n_rays;
 
@@ -1206,10 +1222,10 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 5 : 4) render_kernel(
           acc2 = fmaf(w, fmaxf(__fadd_rn(col[2], 0.5f), 0.f), acc2);
           if (MODE != kFwd) {
             const int idx = n_eval + __popc(s.evm & ((1u << lane) - 1u));
-            if (idx < io.cap) {
-              sm.col[idx * 3 + 0] = col[0];
-              sm.col[idx * 3 + 1] = col[1];
-              sm.col[idx * 3 + 2] = col[2];
+            if (idx < cap) {
+              colc[idx * 3 + 0] = col[0];
+              colc[idx * 3 + 1] = col[1];
+              colc[idx * 3 + 2] = col[2];
             }
           }
         }
@@ -1350,11 +1366,11 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 5 : 4) render_kernel(
           float col[3] = {0.f, 0.f, 0.f};
           float w8[8];
           corner_weights(s.pos[0], s.pos[1], s.pos[2], w8);
-          if (idx0 + __popc(s.evm) <= io.cap) {
+          if (idx0 + __popc(s.evm) <= cap) {
             if (ev) {
-              col[0] = sm.col[(idx0 + rank) * 3 + 0];
-              col[1] = sm.col[(idx0 + rank) * 3 + 1];
-              col[2] = sm.col[(idx0 + rank) * 3 + 2];
+              col[0] = colc[(idx0 + rank) * 3 + 0];
+              col[1] = colc[(idx0 + rank) * 3 + 1];
+              col[2] = colc[(idx0 + rank) * 3 + 2];
             }
           } else {
             // colours past the cache: gather again
@@ -1472,7 +1488,9 @@ int launch_t(const GridP& g, const OptP& opt, IoP io, long long n_rays, cudaStre
   auto kern = render_kernel<BD, ShT, MODE, IMAGE, MULTI, BG>;
   const int cap = MODE == kFwd ? 0 : io.cap;
   io.cap = cap;
-  const size_t smem = sizeof(float) * (size_t)warp_smem_floats(C, cap, MODE != kFwd) * kWarps;
+  if (MODE == kFwd) io.gcol = nullptr;
+  const size_t smem =
+      sizeof(float) * (size_t)warp_smem_floats(C, io.gcol != nullptr ? 0 : cap, MODE != kFwd) * kWarps;
   // per (device, colour-cache capacity): the shared-memory attribute is set on each device the
   // kernel runs on, and the occupancy it allows is looked up once
   static std::mutex mu;
@@ -1482,7 +1500,7 @@ int launch_t(const GridP& g, const OptP& opt, IoP io, long long n_rays, cudaStre
   int bps;
   {
     std::lock_guard<std::mutex> lk(mu);
-    int& slot = blocks_per_sm[std::make_pair(dev, cap)];
+    int& slot = blocks_per_sm[std::make_pair(dev, io.gcol != nullptr ? -1 : cap)];
     if (slot == 0) {
       SVX_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       int b = 0;

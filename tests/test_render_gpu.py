@@ -218,13 +218,14 @@ def test_accelerated_links_skip():
 
 
 def test_adjoint_sample_limit_is_enforced():
-    """A ray may need up to diagonal / step_size samples; beyond the adjoint's 64 x 64
-    checkpointed segments the fused and backward renders refuse on the host, the forward runs."""
+    """A ray may need up to diagonal / step_size samples; beyond what the adjoint's checkpoints
+    cover (64 checkpoints, each at most 64 segments of 32 samples apart: 131,072 samples) the
+    fused and backward renders refuse on the host; the forward runs."""
     from svox2_gb300 import csrc as C
     g = S.make_grid(32, seed=30)
     spec, og = grid_pair(g)
     o, d, gt = S.make_rays(64, seed=31)
-    opt, _ = opt_struct(step=0.01)           # 32 * sqrt(3) / 0.01 ~ 5545 samples > 4096
+    opt, _ = opt_struct(step=0.0004)           # 32 * sqrt(3) / 0.0004 ~ 138,566 samples > 131,072
     rays = rays_pair(o, d)
     N = og.density.shape[0]
     grads = C.GridOutputGrads()
@@ -235,6 +236,31 @@ def test_adjoint_sample_limit_is_enforced():
     with pytest.raises(RuntimeError, match="samples per ray"):
         C.volume_render_cuvol_fused(spec, rays, opt, gt.cuda(), 0.0, 0.0, rgb, grads)
     assert C.volume_render_cuvol(spec, rays, opt).shape == (64, 3)
+
+
+def test_rays_near_the_adjoint_sample_limit():
+    """Rays of ~127,000 evaluated samples, just inside the checkpoints' 131,072: checkpoints
+    thinned to a stride of 64 segments, and colours past the colour cache's 4096 samples
+    gathered again in the reverse pass."""
+    reso = (2, 2, 63500)
+    g = S.make_grid(reso, seed=41, density_mode="normal53")
+    g.density.mul_(1e-5)   # transparent enough that the rays run the whole length
+    spec, og = grid_pair(g)
+    Q = 8
+    gen = torch.Generator().manual_seed(42)
+    o = torch.zeros((Q, 3))
+    o[:, 0] = (torch.rand(Q, generator=gen) - 0.5) * 0.5
+    o[:, 1] = (torch.rand(Q, generator=gen) - 0.5) * 0.5
+    o[:, 2] = -1.2
+    d = torch.zeros((Q, 3))
+    d[:, 0] = (torch.rand(Q, generator=gen) - 0.5) * 1e-6
+    d[:, 1] = (torch.rand(Q, generator=gen) - 0.5) * 1e-6
+    d[:, 2] = 1.0
+    d = d / d.norm(dim=-1, keepdim=True)
+    gt = torch.rand((Q, 3), generator=gen)
+    opt, oopt = opt_struct(stop_thresh=0.0)
+    _, _, ref = _run_fused(spec, og, rays_pair(o, d), o, d, gt, opt, oopt, long_rays=True, label="near limit")
+    assert ref["n_eval"] > Q * 120000
 
 
 def test_invalid_arguments_raise():

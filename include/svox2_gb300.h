@@ -54,7 +54,8 @@ typedef enum { SVX_F32 = 0, SVX_BF16 = 1, SVX_F16 = 2 } svx_dtype;
  *              level written by accel_dist_prop.
  *   density    float32 [n_voxels, 1].
  *   sh         [n_voxels, sh_data_dim] of sh_dtype, channel-major per voxel:
- *              coefficient k of colour channel c is sh[v, c*basis_dim + k].
+ *              coefficient k of colour channel c is sh[v, c*basis_dim + k];
+ *              4-byte aligned (rows are copied in aligned 4-byte words).
  *   offset/scaling  world -> grid transform, grid = world*scaling + offset
  *              (the reference's _offset/_scaling CPU tensors, svox2/svox2.py:2135-2161).
  *   background_nlayers  0, or the layer count (>= 2) of the MSI background model

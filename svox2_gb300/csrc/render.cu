@@ -279,6 +279,9 @@ int check_grid(const svx_grid_t* grid) {
   }
   SVX_REQUIRE(grid->sh_dtype == SVX_F32 || grid->sh_dtype == SVX_BF16 || grid->sh_dtype == SVX_F16,
               SVX_ERR_INVALID, "sh_dtype %d unknown", grid->sh_dtype);
+  // the ray march copies SH rows into shared memory in aligned 4-byte words
+  SVX_REQUIRE((reinterpret_cast<uintptr_t>(grid->sh_data) & 3u) == 0, SVX_ERR_INVALID,
+              "sh_data must be 4-byte aligned (a 16-bit table must not start at an odd element)");
   SVX_REQUIRE(grid->n_voxels >= 0 && grid->n_voxels < (1ll << 31), SVX_ERR_TOO_LARGE,
               "n_voxels %lld must fit int32 links", (long long)grid->n_voxels);
   return SVX_OK;

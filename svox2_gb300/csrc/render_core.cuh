@@ -31,6 +31,7 @@
 #include "common.cuh"
 
 #include <climits>
+#include <type_traits>
 #include <cmath>
 #include <map>
 #include <mutex>
@@ -277,18 +278,30 @@ static __device__ __noinline__ float skip_dist(int32_t link, int l0, int l1, int
 // slots 1..32 hold this segment's runs.
 constexpr int kSlots = 33;
 constexpr int kSlotStride = 33;  // floats per slot (odd: lanes reading different slots hit different banks)
-constexpr int kTileRows = 16;    // coefficient rows gathered per pass (one row per lane in the reduction)
+constexpr int kTileRows = 16;    // coefficient rows gathered per pass, 16-bit SH (loads through registers)
+
+// Coefficient rows gathered per pass.  Rows are copied into shared memory with cp.async, all rows
+// of a pass in flight at once (one memory round trip per pass, no registers held): 32 rows for
+// the adjoint instantiations, 24 for the forward-only ones, whose five blocks per SM leave less
+// shared memory per warp.
+template <typename ShT, int MODE>
+__host__ __device__ constexpr int tile_rows() {
+  return MODE == 0 ? 24 : 32;
+}
+
+// 4-byte words a 16-bit row of C coefficients can span (it starts on a 2-byte boundary).
+__host__ __device__ constexpr int row_words16(int C) { return C / 2 + 1; }
 constexpr int kMaxRows = 8 * 32; // corner rows a segment can need
 constexpr int kFlushCap = 64;    // retiring corner rows listed before a flush pass
 
-__host__ __device__ constexpr int tile_floats(int C) {
-  return kTileRows * C > kFlushCap * 5 ? kTileRows * C : kFlushCap * 5;
+__host__ __device__ constexpr int tile_floats(int C, int rows) {
+  return rows * C > kFlushCap * 5 ? rows * C : kFlushCap * 5;
 }
 
 struct WarpSmem {
   int* links;        // [32][8] corner links of the staged samples
   float* slot;       // [kSlots][kSlotStride]: D[j*3+g] (colour pass) or B[g*8+j] (adjoint)
-  float* tile;       // [kTileRows][C] gathered coefficient rows; in the adjoint, the flush list
+  float* tile;       // [rows][C] gathered coefficient rows; in the adjoint, the flush list
   int* rowlink;      // [kMaxRows] link of each row to gather
   int* rowdst;       // [kMaxRows] slot*8 + corner of each row
   int* run_lane;     // [kSlots] first lane of each run
@@ -307,17 +320,17 @@ struct WarpSmem {
 
 // adjoint: the reverse pass's checkpoint arrays are carved (the forward-only kernel has none,
 // which lets five of its blocks share an SM).
-__host__ __device__ constexpr int warp_smem_floats(int C, int cap, bool adjoint = true) {
-  return (32 * 8 + kSlots * kSlotStride + tile_floats(C) + 2 * kMaxRows + kSlots * 6 +
+__host__ __device__ constexpr int warp_smem_floats(int C, int cap, bool adjoint, int rows) {
+  return (32 * 8 + kSlots * kSlotStride + tile_floats(C, rows) + 2 * kMaxRows + kSlots * 6 +
           (adjoint ? 3 * kNumCkpt + 3 * kMaxStride : 0) + 12 + 3 * cap + 3) & ~3;
 }
 
-__device__ __forceinline__ WarpSmem carve(float* base, int C, int cap, bool adjoint = true) {
+__device__ __forceinline__ WarpSmem carve(float* base, int C, int cap, bool adjoint, int rows) {
   WarpSmem s;
   s.links = reinterpret_cast<int*>(base);
   s.slot = base + 32 * 8;
   s.tile = s.slot + kSlots * kSlotStride;
-  s.rowlink = reinterpret_cast<int*>(s.tile + tile_floats(C));
+  s.rowlink = reinterpret_cast<int*>(s.tile + tile_floats(C, rows));
   s.rowdst = s.rowlink + kMaxRows;
   s.run_lane = s.rowdst + kMaxRows;
   s.run_l = s.run_lane + kSlots;
@@ -557,7 +570,15 @@ __device__ __forceinline__ int segment_runs(const Seg& s, bool have_prev, long l
 // for runs 1..nR.  Corners shared with the previous run (slot r-1; slot 0 is the
 // carried cell when have_prev) are copied, the others gathered: 27 consecutive
 // lanes read one voxel's coefficients, 30 lanes reduce 10 rows x 3 groups.
-template <int BD, typename ShT>
+// 4-byte asynchronous copy global -> shared; src_bytes 0 writes a zero without reading.
+__device__ __forceinline__ void cp_async4(float* dst, const float* src, int src_bytes) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(src), "r"(src_bytes) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+template <int BD, typename ShT, int TR>
 __device__ __forceinline__ void run_colours(int nR, bool have_prev, const WarpSmem& sm, const float basis[9],
                                             const ShT* __restrict__ sh, int lane) {
   constexpr int C = 3 * BD;
@@ -604,32 +625,59 @@ __device__ __forceinline__ void run_colours(int nR, bool have_prev, const WarpSm
     }
   }
   __syncwarp();
-  // gather and reduce, kTileRows rows per pass: loads are issued 8 rows at a time
-  // so that a pass costs one memory round trip
-  for (int m0 = 0; m0 < M; m0 += kTileRows) {
-    const int nrow = min(kTileRows, M - m0);
-    for (int q0 = 0; q0 < nrow; q0 += 8) {
-      float x[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int lk = (q0 + u < nrow) ? sm.rowlink[m0 + q0 + u] : -1;
-        x[u] = (lane < C && lk >= 0) ? ldg_f32(sh + (long long)lk * C + lane) : 0.f;
+  // gather and reduce, TR rows per pass
+  for (int m0 = 0; m0 < M; m0 += TR) {
+    const int nrow = min(TR, M - m0);
+    if constexpr (std::is_same<ShT, float>::value) {
+      // every row of the pass in flight at once: lane k copies coefficient k of each row
+      if (lane < C) {
+        for (int u = 0; u < nrow; ++u) {
+          const int lk = sm.rowlink[m0 + u];
+          cp_async4(sm.tile + u * C + lane, sh + (long long)(lk >= 0 ? lk : 0) * C + lane, lk >= 0 ? 4 : 0);
+        }
+        cp_async_wait_all();
       }
-#pragma unroll
-      for (int u = 0; u < 8; ++u)
-        if (q0 + u < nrow && lane < C) sm.tile[(q0 + u) * C + lane] = x[u];
+    } else {
+      // 16-bit rows start on 2-byte boundaries: lane w copies the w-th aligned 4-byte word that
+      // the row spans.  A row whose last coefficient is the low half of its word copies only
+      // that half (2 bytes), so no word reaches past the row into memory the table may not own.
+      constexpr int W = row_words16(C);
+      if (lane < W) {
+        const float* words = reinterpret_cast<const float*>(sh);
+        for (int u = 0; u < nrow; ++u) {
+          const int lk = sm.rowlink[m0 + u];
+          const long long e0 = (long long)(lk >= 0 ? lk : 0) * C;  // first coefficient (halfwords)
+          const long long wi = (e0 >> 1) + lane, wl = (e0 + C - 1) >> 1;
+          const int bytes = lk < 0 || wi > wl ? 0 : (wi == wl && !((e0 + C - 1) & 1) ? 2 : 4);
+          cp_async4(sm.tile + u * W + lane, words + (bytes ? wi : 0), bytes);
+        }
+        cp_async_wait_all();
+      }
     }
     __syncwarp();
     if (lane < nrow) {
-      const float* row = sm.tile + lane * C;
       const int dst = sm.rowdst[m0 + lane];
       float* out = sm.slot + (dst >> 3) * kSlotStride + (dst & 7) * 3;
+      if constexpr (std::is_same<ShT, float>::value) {
+        const float* row = sm.tile + lane * C;
 #pragma unroll
-      for (int gg = 0; gg < 3; ++gg) {
-        float acc = 0.f;
+        for (int gg = 0; gg < 3; ++gg) {
+          float acc = 0.f;
 #pragma unroll
-        for (int k = 0; k < BD; ++k) acc = fmaf(basis[k], row[gg * BD + k], acc);
-        out[gg] = acc;
+          for (int k = 0; k < BD; ++k) acc = fmaf(basis[k], row[gg * BD + k], acc);
+          out[gg] = acc;
+        }
+      } else {
+        const int lk = sm.rowlink[m0 + lane];
+        const ShT* row = reinterpret_cast<const ShT*>(sm.tile + lane * row_words16(C)) +
+                         (int)(((long long)(lk >= 0 ? lk : 0) * C) & 1);
+#pragma unroll
+        for (int gg = 0; gg < 3; ++gg) {
+          float acc = 0.f;
+#pragma unroll
+          for (int k = 0; k < BD; ++k) acc = fmaf(basis[k], to_f32<ShT>(row[gg * BD + k]), acc);
+          out[gg] = acc;
+        }
       }
     }
     __syncwarp();
@@ -1103,8 +1151,9 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 5 : kAdjointBlocksPer
   // L2 between a ray's forward and reverse passes; sized by the host for the grid's longest ray),
   // or, without one, cap samples in shared memory.  Samples past the capacity are gathered again.
   const int scap = io.gcol != nullptr ? 0 : io.cap;
-  float* wbase = reinterpret_cast<float*>(smem4) + (size_t)wib * warp_smem_floats(C, scap, MODE != kFwd);
-  const WarpSmem sm = carve(wbase, C, scap, MODE != kFwd);
+  constexpr int TR = tile_rows<ShT, MODE>();
+  float* wbase = reinterpret_cast<float*>(smem4) + (size_t)wib * warp_smem_floats(C, scap, MODE != kFwd, TR);
+  const WarpSmem sm = carve(wbase, C, scap, MODE != kFwd, TR);
   const long long gslot = (long long)blockIdx.x * kWarps + wib;
   const bool gown = io.gcol != nullptr && gslot < io.gcol_warps;
   float* colc = gown ? io.gcol + gslot * io.cap * 3 : sm.col;
@@ -1210,7 +1259,7 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 5 : kAdjointBlocksPer
         }
         int slot;
         const int nR = segment_runs(s, have_prev, prev_base, sm, lane, &slot);
-        run_colours<BD, ShT>(nR, have_prev, sm, basis, sh, lane);
+        run_colours<BD, ShT, TR>(nR, have_prev, sm, basis, sh, lane);
         const bool ev = (s.evm >> lane) & 1u;
         if (ev) {
           float w8[8], col[3];
@@ -1374,7 +1423,7 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 5 : kAdjointBlocksPer
             }
           } else {
             // colours past the cache: gather again
-            run_colours<BD, ShT>(nR, false, sm, basis, sh, lane);
+            run_colours<BD, ShT, TR>(nR, false, sm, basis, sh, lane);
             if (ev) lane_colour(sm, slot, w8, col);
           }
           // d(loss)/d(colour) pieces, trace_ray_cuvol_backward cuvol.cu:311-344
@@ -1489,8 +1538,9 @@ int launch_t(const GridP& g, const OptP& opt, IoP io, long long n_rays, cudaStre
   const int cap = MODE == kFwd ? 0 : io.cap;
   io.cap = cap;
   if (MODE == kFwd) io.gcol = nullptr;
-  const size_t smem =
-      sizeof(float) * (size_t)warp_smem_floats(C, io.gcol != nullptr ? 0 : cap, MODE != kFwd) * kWarps;
+  const size_t smem = sizeof(float) *
+                      (size_t)warp_smem_floats(C, io.gcol != nullptr ? 0 : cap, MODE != kFwd, tile_rows<ShT, MODE>()) *
+                      kWarps;
   // per (device, colour-cache capacity): the shared-memory attribute is set on each device the
   // kernel runs on, and the occupancy it allows is looked up once
   static std::mutex mu;

@@ -67,6 +67,16 @@ template <> __device__ __forceinline__ float to_f32<__nv_bfloat16>(__nv_bfloat16
 }
 template <> __device__ __forceinline__ float to_f32<__half>(__half v) { return __half2float(v); }
 
+// A 16-bit table entry from its raw bits: bfloat16 is the top half of a float (a shift, no
+// conversion instruction); float16 goes through the hardware conversion.
+template <typename T> __device__ __forceinline__ float bits16_to_f32(unsigned short b);
+template <> __device__ __forceinline__ float bits16_to_f32<__nv_bfloat16>(unsigned short b) {
+  return __uint_as_float((unsigned)b << 16);
+}
+template <> __device__ __forceinline__ float bits16_to_f32<__half>(unsigned short b) {
+  return __half2float(__ushort_as_half(b));
+}
+
 template <typename T> __device__ __forceinline__ T from_f32(float v);
 template <> __device__ __forceinline__ float from_f32<float>(float v) { return v; }
 template <> __device__ __forceinline__ __nv_bfloat16 from_f32<__nv_bfloat16>(float v) {

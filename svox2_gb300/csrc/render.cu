@@ -449,12 +449,13 @@ static int render_rays(const svx_grid_t* grid, const svx_rays_t* rays, const svx
   if (MODE != kFwd) {
     // The adjoint's colour cache: one slice per resident warp of the launch (the adjoint
     // instantiations are bounded to kAdjointBlocksPerSm blocks per SM), as long as the grid's
-    // longest ray up to kGlobalCapMax samples.  At the 256^3 workload that is 896 samples, about
-    // 26 MB in all, most of it held in L2 between a ray's forward and reverse passes.
+    // longest ray up to kGlobalCapMax samples, 16 bytes per sample.  At the 256^3 workload that
+    // is 896 samples, about 35 MB in all, much of it held in L2 between a ray's forward and
+    // reverse passes.
     const double want = std::ceil(max_samples / 32.0) * 32.0;
     io.cap = (int)std::min(want, (double)kGlobalCapMax);
     io.gcol_warps = (long long)num_sms() * kAdjointBlocksPerSm * kWarps;
-    rc = scr.alloc(3, sizeof(float) * 3 * (size_t)io.cap * (size_t)io.gcol_warps);
+    rc = scr.alloc(3, sizeof(float4) * (size_t)io.cap * (size_t)io.gcol_warps);
     if (rc) return rc;
     io.gcol = reinterpret_cast<float*>(scr.p[3]);
   }

@@ -48,7 +48,9 @@ constexpr int kMaxStride = 64; // checkpoint thinning limit: 64*64 segments per 
 // samples per ray the adjoint's checkpoints cover: kNumCkpt checkpoints, each at most kMaxStride
 // segments (of 32 samples) that hold evaluated samples apart
 constexpr int kMaxAdjointSamples = kNumCkpt * kMaxStride * 32;
-constexpr int kDefaultCap = 192;     // shared-memory colour cache (launches without a global one)
+// shared-memory colour cache (launches without a global one): 48 entries of 16 bytes keep the
+// adjoint instantiations at four blocks per SM
+constexpr int kDefaultCap = 48;
 constexpr int kGlobalCapMax = 4096;  // global colour cache: samples per ray, at most
 constexpr int kAdjointBlocksPerSm = 4;  // __launch_bounds__ of the adjoint instantiations
 constexpr long long kSortMinRays = 1 << 15;  // batches below this run in input order
@@ -308,6 +310,7 @@ struct WarpSmem {
   int* run_l;        // [kSlots][3] cell of each run
   int* run_need;     // [kSlots] corners the run gathers (bit mask)
   int* run_delta;    // [kSlots] index offset of a shared corner in the previous run
+  int* run_walk;     // [kSlots] adjoint: each run's transition from the run after it (walk_info)
   float* ck_t;       // [kNumCkpt]
   float* ck_lt;      // [kNumCkpt]
   int* ck_idx;       // [kNumCkpt]
@@ -315,14 +318,14 @@ struct WarpSmem {
   float* tmp_lt;
   int* tmp_idx;
   float* basis;      // [12] SH basis of the current ray
-  float* col;        // [cap][3]
+  float* col;        // [cap][4] colour cache entries (16-byte aligned)
 };
 
 // adjoint: the reverse pass's checkpoint arrays are carved (the forward-only kernel has none,
 // which lets five of its blocks share an SM).
 __host__ __device__ constexpr int warp_smem_floats(int C, int cap, bool adjoint, int rows) {
-  return (32 * 8 + kSlots * kSlotStride + tile_floats(C, rows) + 2 * kMaxRows + kSlots * 6 +
-          (adjoint ? 3 * kNumCkpt + 3 * kMaxStride : 0) + 12 + 3 * cap + 3) & ~3;
+  return (32 * 8 + kSlots * kSlotStride + tile_floats(C, rows) + 2 * kMaxRows + kSlots * 7 +
+          (adjoint ? 3 * kNumCkpt + 3 * kMaxStride : 0) + 16 + 4 * cap + 3) & ~3;
 }
 
 __device__ __forceinline__ WarpSmem carve(float* base, int C, int cap, bool adjoint, int rows) {
@@ -336,14 +339,15 @@ __device__ __forceinline__ WarpSmem carve(float* base, int C, int cap, bool adjo
   s.run_l = s.run_lane + kSlots;
   s.run_need = s.run_l + 3 * kSlots;
   s.run_delta = s.run_need + kSlots;
-  s.ck_t = reinterpret_cast<float*>(s.run_delta + kSlots);
+  s.run_walk = s.run_delta + kSlots;
+  s.ck_t = reinterpret_cast<float*>(s.run_walk + kSlots);
   s.ck_lt = s.ck_t + kNumCkpt;
   s.ck_idx = reinterpret_cast<int*>(s.ck_lt + kNumCkpt);
   s.tmp_t = reinterpret_cast<float*>(s.ck_idx + kNumCkpt);
   s.tmp_lt = s.tmp_t + kMaxStride;
   s.tmp_idx = reinterpret_cast<int*>(s.tmp_lt + kMaxStride);
   s.basis = adjoint ? reinterpret_cast<float*>(s.tmp_idx + kMaxStride) : s.ck_t;
-  s.col = s.basis + 12;
+  s.col = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(s.basis + 12) + 15) & ~(uintptr_t)15);
   return s;
 }
 
@@ -365,9 +369,15 @@ struct Seg {
   float sigma, pcnt, ws, lt_before, lt_after;
 };
 
+// replay (the adjoint, for a segment whose samples the colour cache holds): the log
+// transmittance before each evaluated sample is the forward's, read from the cache entry of the
+// sample (its index: idx0 plus the evaluated samples before it in the segment), and the
+// forward's early stop is where its count of evaluated samples, n_total, ends; the serial chain
+// of subtractions is not run again.  lt_after = lt_before - pcnt is the forward's same operation.
 __device__ __forceinline__ void march_segment(Seg& s, float t0, float lt0, const RayGeo& r,
                                               const GridP& g, const OptP& opt, int* slinks,
-                                              unsigned long long* trace_h, int lane) {
+                                              unsigned long long* trace_h, int lane,
+                                              const float4* replay = nullptr, int idx0 = 0, int n_total = 0) {
   __syncwarp();  // every lane is done with the previous segment's staged links
   // Sample t: the reference adds step to t once per sample (trace_ray_cuvol's t += step).
   // Lane k's value of that chain equals the single-rounded t0 + k*step whenever every add
@@ -440,6 +450,21 @@ __device__ __forceinline__ void march_segment(Seg& s, float t0, float lt0, const
   s.ws = (opt.last_opaque && __fadd_rn(tk, opt.step) > r.tmax) ? 1e9f : r.world_step;
   s.pcnt = __fmul_rn(s.ws, sigma);
   unsigned evm = __ballot_sync(kFull, normal && sigma > opt.sigma_thresh);
+
+  if (replay != nullptr) {
+    const int idx = idx0 + __popc(evm & ((1u << lane) - 1u));
+    const bool keep = ((evm >> lane) & 1u) && idx < n_total;
+    const unsigned kept = __ballot_sync(kFull, keep);
+    s.stopped = kept != evm;
+    s.lt_before = keep ? replay[idx].w : 0.f;
+    s.lt_after = keep ? __fsub_rn(s.lt_before, s.pcnt) : 0.f;
+    s.evm = kept;
+    s.n = kept ? 32 - __clz(kept) : 0;
+    s.lt_end = 0.f;
+    s.end = true;
+    s.t_next = 0.f;
+    return;
+  }
 
   // Transmittance, evaluated samples in order (cuvol.cu:96-106).  The stop test
   // exp(log T) < stop_thresh is taken as log T < log_stop, log_stop being the
@@ -643,13 +668,14 @@ __device__ __forceinline__ void run_colours(int nR, bool have_prev, const WarpSm
       // that half (2 bytes), so no word reaches past the row into memory the table may not own.
       constexpr int W = row_words16(C);
       if (lane < W) {
-        const float* words = reinterpret_cast<const float*>(sh);
         for (int u = 0; u < nrow; ++u) {
           const int lk = sm.rowlink[m0 + u];
-          const long long e0 = (long long)(lk >= 0 ? lk : 0) * C;  // first coefficient (halfwords)
-          const long long wi = (e0 >> 1) + lane, wl = (e0 + C - 1) >> 1;
-          const int bytes = lk < 0 || wi > wl ? 0 : (wi == wl && !((e0 + C - 1) & 1) ? 2 : 4);
-          cp_async4(sm.tile + u * W + lane, words + (bytes ? wi : 0), bytes);
+          const uintptr_t rb = reinterpret_cast<uintptr_t>(sh + (long long)(lk >= 0 ? lk : 0) * C);
+          const int par = (int)(rb >> 1) & 1;  // the row starts in the high half of a word
+          const float* wp = reinterpret_cast<const float*>(rb & ~(uintptr_t)3);
+          const int nw = (par + C + 1) >> 1;
+          const int bytes = (lk < 0 || lane >= nw) ? 0 : ((lane == nw - 1 && ((par + C) & 1)) ? 2 : 4);
+          cp_async4(sm.tile + u * W + lane, wp + (bytes ? lane : 0), bytes);
         }
         cp_async_wait_all();
       }
@@ -669,13 +695,14 @@ __device__ __forceinline__ void run_colours(int nR, bool have_prev, const WarpSm
         }
       } else {
         const int lk = sm.rowlink[m0 + lane];
-        const ShT* row = reinterpret_cast<const ShT*>(sm.tile + lane * row_words16(C)) +
-                         (int)(((long long)(lk >= 0 ? lk : 0) * C) & 1);
+        // the table starts on a 4-byte boundary, so a row's half-word parity is that of lk * C
+        const unsigned short* row =
+            reinterpret_cast<const unsigned short*>(sm.tile + lane * row_words16(C)) + ((lk & C) & 1);
 #pragma unroll
         for (int gg = 0; gg < 3; ++gg) {
           float acc = 0.f;
 #pragma unroll
-          for (int k = 0; k < BD; ++k) acc = fmaf(basis[k], to_f32<ShT>(row[gg * BD + k]), acc);
+          for (int k = 0; k < BD; ++k) acc = fmaf(basis[k], bits16_to_f32<ShT>(row[gg * BD + k]), acc);
           out[gg] = acc;
         }
       }
@@ -707,6 +734,37 @@ __device__ __forceinline__ void lane_colour(const WarpSmem& sm, int slot, const 
   col[0] = c0;
   col[1] = c1;
   col[2] = c2;
+}
+
+// The adjoint walks a segment's runs last to first, carrying per (group, corner) gradient sums B
+// from one run to the one before it.  walk_info precomputes, for every run q in parallel (lane
+// q - 1), the transition from the run walked before it (run q + 1, or for q = nR the carried cell
+// of the later segment): bits 0-7 the corners of that run that q does not share (they retire),
+// bits 8-15 the corners of q that are new, bits 16-20 the corner index shift 4 dx + 2 dy + dz
+// (plus 16) of the shared ones, bit 21 set when the cell changes.  A run with no run before it
+// in the walk retires nothing.
+constexpr int kWalkTrans = 1 << 21;
+
+__device__ __forceinline__ void walk_info(int nR, bool have_b, const int bcell[3], const WarpSmem& sm, int lane) {
+  const int q = lane + 1;
+  if (q <= nR) {
+    const int c0 = sm.run_l[q * 3 + 0], c1 = sm.run_l[q * 3 + 1], c2 = sm.run_l[q * 3 + 2];
+    const bool has_prev = q < nR || have_b;
+    const int p0 = q < nR ? sm.run_l[(q + 1) * 3 + 0] : bcell[0];
+    const int p1 = q < nR ? sm.run_l[(q + 1) * 3 + 1] : bcell[1];
+    const int p2 = q < nR ? sm.run_l[(q + 1) * 3 + 2] : bcell[2];
+    const int dx = c0 - p0, dy = c1 - p1, dz = c2 - p2;
+    int info = 0;
+    if (!has_prev || dx != 0 || dy != 0 || dz != 0) {
+      const bool near = has_prev && abs(dx) <= 1 && abs(dy) <= 1 && abs(dz) <= 1;
+      const unsigned retire = has_prev ? (near ? new_corner_mask(-dx, -dy, -dz) : 0xFFu) : 0u;
+      const unsigned fresh = near ? new_corner_mask(dx, dy, dz) : 0xFFu;
+      const int delta = near ? 4 * dx + 2 * dy + dz : 0;
+      info = kWalkTrans | (int)retire | (int)(fresh << 8) | ((delta + 16) << 16);
+    }
+    sm.run_walk[q] = info;
+  }
+  __syncwarp();
 }
 
 // The adjoint lists retiring corners (their 4 accumulators and link) in shared
@@ -1150,13 +1208,15 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 5 : kAdjointBlocksPer
   // The adjoint's per-sample colour cache: a slice of io.gcol (global memory, most of it held in
   // L2 between a ray's forward and reverse passes; sized by the host for the grid's longest ray),
   // or, without one, cap samples in shared memory.  Samples past the capacity are gathered again.
-  const int scap = io.gcol != nullptr ? 0 : io.cap;
+  const int scap = io.gcol != nullptr ? 0 : io.cap;  // samples in the shared-memory cache
   constexpr int TR = tile_rows<ShT, MODE>();
   float* wbase = reinterpret_cast<float*>(smem4) + (size_t)wib * warp_smem_floats(C, scap, MODE != kFwd, TR);
   const WarpSmem sm = carve(wbase, C, scap, MODE != kFwd, TR);
   const long long gslot = (long long)blockIdx.x * kWarps + wib;
   const bool gown = io.gcol != nullptr && gslot < io.gcol_warps;
-  float* colc = gown ? io.gcol + gslot * io.cap * 3 : sm.col;
+  // one float4 per evaluated sample: its colour (before the +0.5 offset) and the log
+  // transmittance before it
+  float4* colc = reinterpret_cast<float4*>(gown ? io.gcol + gslot * io.cap * 4 : sm.col);
   const int cap = (io.gcol == nullptr || gown) ? io.cap : 0;
   const int grp = lane >> 3, cj = lane & 7;
   const long long n_rays = MULTI ? *io.n_rays_dev : io.n_rays;
@@ -1271,11 +1331,7 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 5 : kAdjointBlocksPer
           acc2 = fmaf(w, fmaxf(__fadd_rn(col[2], 0.5f), 0.f), acc2);
           if (MODE != kFwd) {
             const int idx = n_eval + __popc(s.evm & ((1u << lane) - 1u));
-            if (idx < cap) {
-              colc[idx * 3 + 0] = col[0];
-              colc[idx * 3 + 1] = col[1];
-              colc[idx * 3 + 2] = col[2];
-            }
+            if (idx < cap) colc[idx] = make_float4(col[0], col[1], col[2], s.lt_before);
           }
         }
         // carry the last run to the next segment (after every lane has read the slots)
@@ -1406,7 +1462,9 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 5 : kAdjointBlocksPer
           Seg s;
           const float t0 = sm.tmp_t[b], lt0 = sm.tmp_lt[b];
           const int idx0 = sm.tmp_idx[b];
-          march_segment(s, t0, lt0, rg, g, opt, sm.links, nullptr, lane);
+          // segments the colour cache holds replay the forward's transmittance
+          const bool cached = idx0 + 32 <= cap;
+          march_segment(s, t0, lt0, rg, g, opt, sm.links, nullptr, lane, cached ? colc : nullptr, idx0, n_eval);
           __syncwarp();
           int slot;
           const int nR = segment_runs(s, false, 0, sm, lane, &slot);
@@ -1417,9 +1475,10 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 5 : kAdjointBlocksPer
           corner_weights(s.pos[0], s.pos[1], s.pos[2], w8);
           if (idx0 + __popc(s.evm) <= cap) {
             if (ev) {
-              col[0] = colc[(idx0 + rank) * 3 + 0];
-              col[1] = colc[(idx0 + rank) * 3 + 1];
-              col[2] = colc[(idx0 + rank) * 3 + 2];
+              const float4 e = colc[idx0 + rank];
+              col[0] = e.x;
+              col[1] = e.y;
+              col[2] = e.z;
             }
           } else {
             // colours past the cache: gather again
@@ -1472,14 +1531,13 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 5 : kAdjointBlocksPer
           float* fl_val = sm.tile;
           int* fl_link = reinterpret_cast<int*>(sm.tile + kFlushCap * 4);
           int F = 0;
+          walk_info(nR, have_b, bcell, sm, lane);
           for (int q = nR; q >= 1; --q) {
-            const int to0 = sm.run_l[q * 3 + 0], to1 = sm.run_l[q * 3 + 1], to2 = sm.run_l[q * 3 + 2];
-            if (!have_b || to0 != bcell[0] || to1 != bcell[1] || to2 != bcell[2]) {
-              const int dx = to0 - bcell[0], dy = to1 - bcell[1], dz = to2 - bcell[2];
-              const bool near = have_b && abs(dx) <= 1 && abs(dy) <= 1 && abs(dz) <= 1;
-              if (have_b) {
-                // old corners not shared with the new cell: those on the faces -d moved across
-                const unsigned retire = near ? new_corner_mask(-dx, -dy, -dz) : 0xFFu;
+            const int info = sm.run_walk[q];
+            if (info & kWalkTrans) {
+              // old corners not shared with the new cell (those on the faces it moved across) retire
+              const unsigned retire = (unsigned)info & 0xFFu;
+              if (retire) {
                 if (F + 8 > kFlushCap) {
                   if (go.accum != nullptr)
                     flush_list_vec<BD>(F, fl_val, fl_link, sm.basis, go.accum, go.accum_stride, go.mask, lane);
@@ -1490,17 +1548,19 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 5 : kAdjointBlocksPer
                 list_retiring(retire, B, lk_lane, fl_val, fl_link, F, lane);
                 F += __popc(retire);
               }
-              const bool fresh = !near || ((new_corner_mask(dx, dy, dz) >> cj) & 1u);
-              const int src = fresh ? lane : grp * 8 + cj + 4 * dx + 2 * dy + dz;
-              const float moved = __shfl_sync(kFull, B, src);
+              const bool fresh = (info >> (8 + cj)) & 1;
+              const int delta = ((info >> 16) & 31) - 16;
+              const float moved = __shfl_sync(kFull, B, fresh ? lane : lane + delta);
               B = fresh ? 0.f : moved;
               lk_lane = sm.links[sm.run_lane[q] * 8 + cj];
-              bcell[0] = to0;
-              bcell[1] = to1;
-              bcell[2] = to2;
-              have_b = true;
             }
             B = __fadd_rn(B, sm.slot[q * kSlotStride + lane]);
+          }
+          if (nR > 0) {
+            bcell[0] = sm.run_l[3];
+            bcell[1] = sm.run_l[4];
+            bcell[2] = sm.run_l[5];
+            have_b = true;
           }
           if (go.accum != nullptr)
             flush_list_vec<BD>(F, fl_val, fl_link, sm.basis, go.accum, go.accum_stride, go.mask, lane);

@@ -666,16 +666,19 @@ __device__ __forceinline__ void run_colours(int nR, bool have_prev, const WarpSm
       // 16-bit rows start on 2-byte boundaries: lane w copies the w-th aligned 4-byte word that
       // the row spans.  A row whose last coefficient is the low half of its word copies only
       // that half (2 bytes), so no word reaches past the row into memory the table may not own.
+      // A row spans at most 16 words, so the two half-warps copy two rows per step.
       constexpr int W = row_words16(C);
-      if (lane < W) {
-        for (int u = 0; u < nrow; ++u) {
+      static_assert(W <= 16, "a 16-bit row must fit a half-warp");
+      const int half = lane >> 4, wl = lane & 15;
+      if (wl < W) {
+        for (int u = half; u < nrow; u += 2) {
           const int lk = sm.rowlink[m0 + u];
           const uintptr_t rb = reinterpret_cast<uintptr_t>(sh + (long long)(lk >= 0 ? lk : 0) * C);
           const int par = (int)(rb >> 1) & 1;  // the row starts in the high half of a word
           const float* wp = reinterpret_cast<const float*>(rb & ~(uintptr_t)3);
           const int nw = (par + C + 1) >> 1;
-          const int bytes = (lk < 0 || lane >= nw) ? 0 : ((lane == nw - 1 && ((par + C) & 1)) ? 2 : 4);
-          cp_async4(sm.tile + u * W + lane, wp + (bytes ? lane : 0), bytes);
+          const int bytes = (lk < 0 || wl >= nw) ? 0 : ((wl == nw - 1 && ((par + C) & 1)) ? 2 : 4);
+          cp_async4(sm.tile + u * W + wl, wp + (bytes ? wl : 0), bytes);
         }
         cp_async_wait_all();
       }

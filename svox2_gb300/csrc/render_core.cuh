@@ -311,6 +311,7 @@ struct WarpSmem {
   int* run_need;     // [kSlots] corners the run gathers (bit mask)
   int* run_delta;    // [kSlots] index offset of a shared corner in the previous run
   int* run_walk;     // [kSlots] adjoint: each run's transition from the run after it (walk_info)
+  float* pc;         // [32] forward-only march: the segment's optical depths (0 where not evaluated)
   float* ck_t;       // [kNumCkpt]
   float* ck_lt;      // [kNumCkpt]
   int* ck_idx;       // [kNumCkpt]
@@ -324,14 +325,15 @@ struct WarpSmem {
 // adjoint: the reverse pass's checkpoint arrays are carved (the forward-only kernel has none,
 // which lets five of its blocks share an SM).
 __host__ __device__ constexpr int warp_smem_floats(int C, int cap, bool adjoint, int rows) {
-  return (32 * 8 + kSlots * kSlotStride + tile_floats(C, rows) + 2 * kMaxRows + kSlots * 7 +
+  return (32 * 8 + 32 + kSlots * kSlotStride + tile_floats(C, rows) + 2 * kMaxRows + kSlots * 7 +
           (adjoint ? 3 * kNumCkpt + 3 * kMaxStride : 0) + 16 + 4 * cap + 3) & ~3;
 }
 
 __device__ __forceinline__ WarpSmem carve(float* base, int C, int cap, bool adjoint, int rows) {
   WarpSmem s;
   s.links = reinterpret_cast<int*>(base);
-  s.slot = base + 32 * 8;
+  s.pc = base + 32 * 8;
+  s.slot = base + 32 * 8 + 32;
   s.tile = s.slot + kSlots * kSlotStride;
   s.rowlink = reinterpret_cast<int*>(s.tile + tile_floats(C, rows));
   s.rowdst = s.rowlink + kMaxRows;
@@ -369,11 +371,18 @@ struct Seg {
   float sigma, pcnt, ws, lt_before, lt_after;
 };
 
+// SCAN (the forward-only instantiations): every lane forms its own log transmittance from the
+// segment's optical depths, broadcast through shared memory (slinks + 256, the pc array), by the
+// same subtractions in the same order as the serial chain (a sample that is not evaluated
+// contributes 0, and x - 0 == x), so the values are identical; the lanes run the chain in
+// parallel instead of one shuffle per evaluated sample.  The adjoint instantiations keep the
+// serial chain: the scan's extra code slows the fused kernel, which waits on instruction fetch.
 // replay (the adjoint, for a segment whose samples the colour cache holds): the log
 // transmittance before each evaluated sample is the forward's, read from the cache entry of the
 // sample (its index: idx0 plus the evaluated samples before it in the segment), and the
 // forward's early stop is where its count of evaluated samples, n_total, ends; the serial chain
 // of subtractions is not run again.  lt_after = lt_before - pcnt is the forward's same operation.
+template <bool SCAN = false>
 __device__ __forceinline__ void march_segment(Seg& s, float t0, float lt0, const RayGeo& r,
                                               const GridP& g, const OptP& opt, int* slinks,
                                               unsigned long long* trace_h, int lane,
@@ -473,19 +482,54 @@ __device__ __forceinline__ void march_segment(Seg& s, float t0, float lt0, const
   s.lt_before = 0.f;
   s.lt_after = 0.f;
   s.stopped = false;
-  unsigned m = evm;
-  while (m) {
-    const int i = __ffs(m) - 1;
-    m &= m - 1;
-    const float pc = __shfl_sync(kFull, s.pcnt, i);
-    if (lane == i) s.lt_before = lt;
-    lt = __fsub_rn(lt, pc);
-    if (lane == i) s.lt_after = lt;
-    if (lt < opt.log_stop) {
+  if (SCAN) {
+    float* spc = reinterpret_cast<float*>(slinks + 32 * 8);
+    const bool evl = (evm >> lane) & 1u;
+    const float mine = evl ? s.pcnt : 0.f;
+    spc[lane] = mine;
+    __syncwarp();
+    const float4* pc4 = reinterpret_cast<const float4*>(spc);
+    float x = lt0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const float4 v = pc4[q];
+      const int j = 4 * q;
+      x = j + 0 < lane ? __fsub_rn(x, v.x) : x;
+      x = j + 1 < lane ? __fsub_rn(x, v.y) : x;
+      x = j + 2 < lane ? __fsub_rn(x, v.z) : x;
+      x = j + 3 < lane ? __fsub_rn(x, v.w) : x;
+    }
+    __syncwarp();
+    const float xa = __fsub_rn(x, mine);
+    const unsigned sb = __ballot_sync(kFull, evl && xa < opt.log_stop);
+    if (sb) {
+      const int i = __ffs(sb) - 1;
       s.stopped = true;
       s.n = i + 1;
       evm &= (i == 31) ? kFull : ((2u << i) - 1u);
-      break;
+      lt = __shfl_sync(kFull, xa, i);
+    } else if (evm) {
+      lt = __shfl_sync(kFull, xa, 31 - __clz(evm));
+    }
+    if ((evm >> lane) & 1u) {
+      s.lt_before = x;
+      s.lt_after = xa;
+    }
+  } else {
+    unsigned m = evm;
+    while (m) {
+      const int i = __ffs(m) - 1;
+      m &= m - 1;
+      const float pc = __shfl_sync(kFull, s.pcnt, i);
+      if (lane == i) s.lt_before = lt;
+      lt = __fsub_rn(lt, pc);
+      if (lane == i) s.lt_after = lt;
+      if (lt < opt.log_stop) {
+        s.stopped = true;
+        s.n = i + 1;
+        evm &= (i == 31) ? kFull : ((2u << i) - 1u);
+        break;
+      }
     }
   }
   s.evm = evm;
@@ -1292,7 +1336,7 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 5 : kAdjointBlocksPer
     bool stopped = false;
     while (t <= rg.tmax) {
       Seg s;
-      march_segment(s, t, lt, rg, g, opt, sm.links, thp, lane);
+      march_segment<MODE == kFwd>(s, t, lt, rg, g, opt, sm.links, thp, lane);
       if (s.evm) {
         if (MODE != kFwd) {
           // checkpoint the segment (thinned to every stride-th evaluated segment)

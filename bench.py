@@ -805,12 +805,15 @@ def main():
     ap.add_argument("--bg-layers", type=int, default=64, help="background: MSI layers (the T&T configuration's 64)")
     ap.add_argument("--bg-reso", type=int, default=1024, help="background: MSI resolution (T&T: 1024)")
     ap.add_argument("--rate", type=float, default=2000.0, help="serve: Poisson arrival rate (requests/s)")
+    ap.add_argument("--rates", default="", help="serve: comma-separated arrival rates, one line each (overrides --rate)")
     args = ap.parse_args()
     if args.config == "mixed":
         run_mixed(args)
         return
     if args.config == "serve":
-        run_serve(args)
+        for rate in ([float(x) for x in args.rates.split(",")] if args.rates else [args.rate]):
+            args.rate = rate
+            run_serve(args)
         return
     if args.config == "render":
         run_render(args)

@@ -292,7 +292,6 @@ class RenderServer:
         self.opt = _lib.SvxRenderOpts(background_brightness, step_size, sigma_thresh, stop_thresh, 0.0, 0, 0)
         self.use_graphs = use_graphs
         self.dtype = None
-        self.copy_stream = torch.cuda.Stream(device=self.device)
         self.desc_size = C.sizeof(_lib.SvxBatchGrid)
         self.desc_host = np.zeros((max_grids, self.desc_size), dtype=np.uint8)
         B = batch_rays
@@ -308,12 +307,17 @@ class RenderServer:
                 "n_rays": torch.zeros((1,), dtype=torch.int64, device=dev),
                 "work": torch.zeros((4,), dtype=torch.int64, device=dev),
                 "desc": torch.zeros((max_grids, self.desc_size), dtype=torch.uint8, device=dev),
+                "desc_version": -1,      # version of desc_host last uploaded to this lane
                 "graph": None,
             }
         lane_bytes = sum(t.numel() * t.element_size() for lane in self.lanes.values() for t in lane.values()
                          if isinstance(t, torch.Tensor))
         self.sched.budget -= lane_bytes
         self.slots_free = list(range(max_grids))
+        # desc_host versions: any change (train steps rewrite their grid's loss scale) and changes
+        # of the grids themselves (the render lane reads only those)
+        self.desc_version = 0
+        self.grid_version = 0
         self.with_bg = False             # some resident grid has an MSI background
         self.batches = {"render": 0, "train": 0}
         self.accum_min_rays = 1 << 15  # train steps this large accumulate into padded rows (vector atomics)
@@ -350,11 +354,13 @@ class RenderServer:
                 grid._grad_buffer(grid.background_data)
         self.grids[grid_id] = g
         self._set_desc(grid_id, 0.0)
+        self.grid_version += 1
         self._update_background_flag()
 
     def remove_grid(self, grid_id: str) -> None:
         self.sched.remove_grid(grid_id)
         self.slots_free.append(self.grids.pop(grid_id)["slot"])
+        self.grid_version += 1
         self._update_background_flag()
 
     def _update_background_flag(self) -> None:
@@ -382,6 +388,7 @@ class RenderServer:
                 d.accum_stride = g["accum"].size(1)
         d.norm = norm
         self.desc_host[g["slot"]] = np.frombuffer(bytes(d), dtype=np.uint8)
+        self.desc_version += 1
 
     # -- requests
     def submit(self, req, now: Optional[float] = None, timeout: Optional[float] = None) -> Ticket:
@@ -420,11 +427,13 @@ class RenderServer:
         r = t.request
         lane = self.lanes[t.kind]
         with torch.cuda.stream(lane["stream"]):
+            # the result lands in pinned host memory, copied from the lane's output buffer right
+            # after the launch that computed it
+            t.buf["host"] = torch.empty((t.n_rays, 3), dtype=torch.float32, pin_memory=True)
             if t.kind == "render":
                 n = t.n_rays
                 t.buf["origins"] = torch.empty((n, 3), device=self.device)
                 t.buf["dirs"] = torch.empty((n, 3), device=self.device)
-                t.buf["out"] = torch.empty((n, 3), device=self.device)
                 m = np.ascontiguousarray(torch.as_tensor(r.c2w, dtype=torch.float32).cpu().numpy())
                 c2w = torch.empty(m.shape, dtype=torch.float32, device=self.device)
                 self._upload(c2w.view(-1).view(torch.uint8), m)
@@ -439,7 +448,6 @@ class RenderServer:
             else:
                 for k in ("origins", "dirs", "rgb_gt"):
                     t.buf[k] = getattr(r, k).to(self.device, non_blocking=True).contiguous()
-                t.buf["out"] = torch.empty((t.n_rays, 3), device=self.device)
 
     def _launch(self, name: str, n: int) -> None:
         """One batched kernel launch on the lane's current stream: replay of the lane's captured
@@ -447,7 +455,12 @@ class RenderServer:
         lane = self.lanes[name]
         _lib = self._lib
         lane["n_rays"].fill_(n)
-        self._upload(lane["desc"].view(-1), self.desc_host)
+        # the descriptors are uploaded only when they changed since this lane's last upload (the
+        # render lane reads only the grids' tables, not the train steps' loss scales)
+        version = self.desc_version if name == "train" else self.grid_version
+        if lane["desc_version"] != version:
+            self._upload(lane["desc"].view(-1), self.desc_host)
+            lane["desc_version"] = version
         dt = {torch.float32: _lib.SVX_F32, torch.bfloat16: _lib.SVX_BF16, torch.float16: _lib.SVX_F16}[self.dtype]
         mode = 0 if name == "render" else 1
 
@@ -524,7 +537,8 @@ class RenderServer:
             off = 0
             for ch in chunks:
                 t = ch.ticket
-                t.buf["out"][ch.start:ch.start + ch.count].copy_(lane["rgb_out"][off:off + ch.count])
+                t.buf["host"][ch.start:ch.start + ch.count].copy_(lane["rgb_out"][off:off + ch.count],
+                                                                  non_blocking=True)
                 off += ch.count
             ev = torch.cuda.Event()
             ev.record(st)
@@ -569,7 +583,7 @@ class RenderServer:
             for t in trains:
                 g = self.grids[t.grid_id]
                 grid, r = g["grid"], t.request
-                t.buf["out"].copy_(lane["rgb_out"][off:off + t.n_rays])
+                t.buf["host"].copy_(lane["rgb_out"][off:off + t.n_rays], non_blocking=True)
                 off += t.n_rays
                 if t.buf["accum"]:
                     # padded accumulation rows -> the grid's gradients
@@ -605,30 +619,21 @@ class RenderServer:
         lane["queued"].append(ev)
 
     def _collect(self) -> List[Ticket]:
-        """Finish requests whose work completed: results are copied to pinned host memory on a
-        copy stream, and the request finishes when that copy has landed."""
+        """Finish requests whose work completed: each launch copied its part of a result into the
+        request's pinned host buffer on the lane's stream, so the result is there once every
+        launch of the request has completed."""
         done = []
         for t in list(self.sched.active):
-            if "host_ev" in t.buf:
-                if t.buf["host_ev"].query():
-                    out = t.buf["host"]
-                    t.result = out.view(t.request.height, t.request.width, 3) if t.kind == "render" else out
-                    t.buf.clear()
-                    t.rays_done_event.clear()
-                    self.sched.finish(t, time.perf_counter())
-                    done.append(t)
-                continue
             if t.rays_launched < t.n_rays or not t.rays_done_event:
                 continue
             if not all(e.query() for e in t.rays_done_event):
                 continue
-            with torch.cuda.stream(self.copy_stream):
-                h = torch.empty(t.buf["out"].shape, dtype=torch.float32, pin_memory=True)
-                h.copy_(t.buf["out"], non_blocking=True)
-                e = torch.cuda.Event()
-                e.record(self.copy_stream)
-            t.buf["host"] = h
-            t.buf["host_ev"] = e
+            out = t.buf["host"]
+            t.result = out.view(t.request.height, t.request.width, 3) if t.kind == "render" else out
+            t.buf.clear()
+            t.rays_done_event.clear()
+            self.sched.finish(t, time.perf_counter())
+            done.append(t)
         return done
 
     def idle(self) -> bool:

@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define SVX_ABI_VERSION 1
+#define SVX_ABI_VERSION 2
 
 /* Status codes.  The reference raised RuntimeError through TORCH_CHECK
  * (svox2/csrc/include/data_spec.hpp:32-51); the ABI returns these instead and
@@ -255,12 +255,24 @@ typedef struct {
  *               permutation of 0..n_rays-1 (see svx_ray_order).  Outputs stay
  *               at each ray's own index.
  *   work        device uint64 scratch of the caller (cleared by the call)
+ *   colour_cache  NULL, or device memory of colour_cache_bytes (16-byte
+ *               aligned) in which the fused mode keeps each ray's per-sample
+ *               colours for its reverse pass; svx_batch_colour_cache_bytes(n)
+ *               sizes it for rays of up to n evaluated samples.  Without it
+ *               (or when it is too small for 32 samples a ray) the cache is
+ *               48 samples in shared memory, and longer rays gather their
+ *               colours again.
  * Allocates nothing.  max_rays sizes the persistent grid. */
 int svx_render_batch(int32_t mode, const svx_batch_grid_t* grids, int32_t basis_dim, int32_t sh_dtype,
                      int32_t with_background, const float* origins, const float* dirs, const int32_t* ray_grid,
                      const int32_t* order, const int64_t* n_rays_dev, int64_t max_rays,
                      const svx_render_opts_t* opt, const float* rgb_gt, float* rgb_out, uint64_t* work,
-                     void* stream);
+                     float* colour_cache, int64_t colour_cache_bytes, void* stream);
+
+/* Bytes of a svx_render_batch colour cache that holds samples_per_ray
+ * evaluated samples for every warp the batch launch keeps resident on the
+ * current device (16 bytes a sample). */
+int64_t svx_batch_colour_cache_bytes(int32_t samples_per_ray);
 
 /* Coherence order of a ray table against one grid: order_out[i] = index_base +
  * the index of the i-th ray sorted by (octahedral direction bucket, Morton code

@@ -14,7 +14,7 @@ from pathlib import Path
 
 from . import _build
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 
 SVX_OK = 0
 SVX_ERR_INVALID = 1
@@ -111,7 +111,8 @@ SIGNATURES = {
     "svx_volume_render_cuvol_fused_noalloc": [P(SvxGrid), P(SvxRays), P(SvxRenderOpts), _vp, _f32, _f32, _vp,
                                               P(SvxGridGrads), P(SvxRenderStats), _vp],
     "svx_render_batch": [_i32, _vp, _i32, _i32, _i32, _vp, _vp, _vp, _vp, _vp, _i64, P(SvxRenderOpts), _vp, _vp,
-                         _vp, _vp],
+                         _vp, _vp, _i64, _vp],
+    "svx_batch_colour_cache_bytes": [_i32],
     "svx_ray_order": [P(SvxGrid), P(SvxRays), P(SvxRenderOpts), _i32, _vp, _vp],
     "svx_add_accum": [_vp, _i32, _i32, _i64, _vp, _vp, _vp],
     "svx_camera_rays": [P(SvxCamera), _vp, _vp, _vp],
@@ -161,7 +162,8 @@ def load() -> C.CDLL:
         for name, argtypes in SIGNATURES.items():
             fn = getattr(lib, name)
             fn.argtypes = argtypes
-            fn.restype = C.c_char_p if name == "svx_last_error" else C.c_int
+            fn.restype = (C.c_char_p if name == "svx_last_error" else
+                          C.c_int64 if name == "svx_batch_colour_cache_bytes" else C.c_int)
         v = lib.svx_abi_version()
         if v != ABI_VERSION:
             raise ImportError(f"libsvox2_gb300 ABI version {v}, expected {ABI_VERSION}; rebuild the library")

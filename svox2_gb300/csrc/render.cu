@@ -744,7 +744,7 @@ extern "C" int svx_render_batch(int32_t mode, const svx_batch_grid_t* grids, int
                                 int32_t with_background, const float* origins, const float* dirs, const int32_t* ray_grid,
                                 const int32_t* order, const int64_t* n_rays_dev, int64_t max_rays,
                                 const svx_render_opts_t* opt, const float* rgb_gt, float* rgb_out, uint64_t* work,
-                                void* stream) {
+                                float* colour_cache, int64_t colour_cache_bytes, void* stream) {
   clear_error();
   SVX_REQUIRE(mode == 0 || mode == 1, SVX_ERR_INVALID, "mode %d: 0 (render) or 1 (fused)", mode);
   SVX_REQUIRE(basis_dim == 9, SVX_ERR_UNSUPPORTED, "batched launches are built for basis_dim 9");
@@ -768,6 +768,17 @@ extern "C" int svx_render_batch(int32_t mode, const svx_batch_grid_t* grids, int
   io.n_rays_dev = reinterpret_cast<const long long*>(n_rays_dev);
   io.work = reinterpret_cast<unsigned long long*>(work);
   io.cap = g_cap;
+  if (mode == 1 && colour_cache != nullptr) {
+    SVX_REQUIRE((reinterpret_cast<uintptr_t>(colour_cache) & 15u) == 0, SVX_ERR_INVALID,
+                "colour_cache must be 16-byte aligned");
+    const long long warps = (long long)num_sms() * kAdjointBlocksPerSm * kWarps;
+    const long long cap = colour_cache_bytes / (long long)sizeof(float4) / warps;
+    if (cap >= 32) {
+      io.gcol = colour_cache;
+      io.gcol_warps = warps;
+      io.cap = (int)std::min<long long>(cap, kGlobalCapMax);
+    }
+  }
   GridP g{};  // per-ray grids come from the descriptors
   cudaStream_t st = as_stream(stream);
   if (with_background) return dispatch_bg_batch(mode == 0 ? kFwd : kFused, sh_dtype, g, o, io, max_rays, st);
@@ -784,6 +795,11 @@ extern "C" int svx_render_batch(int32_t mode, const svx_batch_grid_t* grids, int
   }
   set_error("sh_dtype %d unknown", sh_dtype);
   return SVX_ERR_INVALID;
+}
+
+extern "C" int64_t svx_batch_colour_cache_bytes(int32_t samples_per_ray) {
+  if (samples_per_ray <= 0) return 0;
+  return (int64_t)num_sms() * kAdjointBlocksPerSm * kWarps * (int64_t)samples_per_ray * (int64_t)sizeof(float4);
 }
 
 extern "C" int svx_ray_order(const svx_grid_t* grid, const svx_rays_t* rays, const svx_render_opts_t* opt,

@@ -310,6 +310,10 @@ class RenderServer:
                 "desc_version": -1,      # version of desc_host last uploaded to this lane
                 "graph": None,
             }
+        # the train lane's colour cache: per-sample colours of rays up to 1024 evaluated samples
+        # (the longest ray of a 256^3 grid at step 0.5 has 887 samples)
+        cache_bytes = int(_lib.load().svx_batch_colour_cache_bytes(1024))
+        self.lanes["train"]["colour_cache"] = torch.empty((cache_bytes // 4,), dtype=torch.float32, device=dev)
         lane_bytes = sum(t.numel() * t.element_size() for lane in self.lanes.values() for t in lane.values()
                          if isinstance(t, torch.Tensor))
         self.sched.budget -= lane_bytes
@@ -466,12 +470,16 @@ class RenderServer:
 
         order = lane["order"].data_ptr() if name == "train" else None
 
+        cache = lane.get("colour_cache")
+
         def call():
             _lib.call("svx_render_batch", mode, lane["desc"].data_ptr(), 9, dt, int(self.with_bg),
                       lane["origins"].data_ptr(),
                       lane["dirs"].data_ptr(), lane["ray_grid"].data_ptr(), order, lane["n_rays"].data_ptr(),
                       self.sched.batch_rays, C.byref(self.opt), lane["rgb_gt"].data_ptr(),
-                      lane["rgb_out"].data_ptr(), lane["work"].data_ptr(), torch.cuda.current_stream().cuda_stream)
+                      lane["rgb_out"].data_ptr(), lane["work"].data_ptr(),
+                      None if cache is None else cache.data_ptr(),
+                      0 if cache is None else cache.numel() * 4, torch.cuda.current_stream().cuda_stream)
 
         self.batches[name] += 1
         if not self.use_graphs:

@@ -67,11 +67,11 @@ def test_new_entry_points_validate_on_the_host():
                                             None), _lib.SVX_ERR_INVALID, b"null"),
         (lambda: lib.svx_camera_rays(None, None, None, None), _lib.SVX_ERR_INVALID, b"null"),
         (lambda: lib.svx_render_batch(0, None, 9, _lib.SVX_F32, 1, None, None, None, None, None, 16, None, None,
-                                      None, None, None), _lib.SVX_ERR_INVALID, b"null"),
+                                      None, None, None, 0, None), _lib.SVX_ERR_INVALID, b"null"),
         (lambda: lib.svx_render_batch(1, None, 4, _lib.SVX_F32, 1, None, None, None, None, None, 16, None, None,
-                                      None, None, None), _lib.SVX_ERR_UNSUPPORTED, b"basis_dim"),
+                                      None, None, None, 0, None), _lib.SVX_ERR_UNSUPPORTED, b"basis_dim"),
         (lambda: lib.svx_render_batch(2, None, 9, _lib.SVX_F32, 0, None, None, None, None, None, 16, None, None,
-                                      None, None, None), _lib.SVX_ERR_INVALID, b"mode"),
+                                      None, None, None, 0, None), _lib.SVX_ERR_INVALID, b"mode"),
     ]
     for call, status, word in cases:
         assert call() == status, lib.svx_last_error()

@@ -40,7 +40,7 @@ def _order(spec, o, d, opt, base, out):
               base, out.data_ptr(), torch.cuda.current_stream().cuda_stream)
 
 
-def _batch(mode, grids, rays, opt, sh_dtype, use_order, accum_for=(), with_bg=0):
+def _batch(mode, grids, rays, opt, sh_dtype, use_order, accum_for=(), with_bg=0, cache_samples=0):
     """One svx_render_batch launch over every grid's rays; returns rgb per grid and the
     per-grid gradient buffers (accumulation rows already flushed)."""
     dev = "cuda"
@@ -82,10 +82,15 @@ def _batch(mode, grids, rays, opt, sh_dtype, use_order, accum_for=(), with_bg=0)
     rgb = torch.zeros((n, 3), device=dev)
     dt = {torch.float32: _lib.SVX_F32, torch.bfloat16: _lib.SVX_BF16, torch.float16: _lib.SVX_F16}[sh_dtype]
     st = torch.cuda.current_stream().cuda_stream
+    cache = None
+    if cache_samples:
+        nbytes = int(_lib.load().svx_batch_colour_cache_bytes(cache_samples))
+        cache = torch.empty((nbytes // 4,), dtype=torch.float32, device=dev)
     _lib.call("svx_render_batch", mode, table.data_ptr(), 9, dt, with_bg, O_.data_ptr(), D_.data_ptr(),
               ray_grid.data_ptr(),
               order.data_ptr() if use_order else None, n_dev.data_ptr(), n, C.byref(csrc._opt_struct(opt)),
-              GT.data_ptr() if mode == 1 else None, rgb.data_ptr(), work.data_ptr(), st)
+              GT.data_ptr() if mode == 1 else None, rgb.data_ptr(), work.data_ptr(),
+              None if cache is None else cache.data_ptr(), 0 if cache is None else cache.numel() * 4, st)
     for (spec, _), b in zip(grids, bufs):
         if "accum" in b:
             _lib.call("svx_add_accum", b["accum"].data_ptr(), b["accum"].size(1), spec.sh_data.size(1),
@@ -100,12 +105,15 @@ def _batch(mode, grids, rays, opt, sh_dtype, use_order, accum_for=(), with_bg=0)
     return out, bufs
 
 
+@pytest.mark.parametrize("cache_samples", [0, 64], ids=["smem_cache", "global_cache"])
 @pytest.mark.parametrize("sh_dtype", [torch.float32, torch.bfloat16])
 @pytest.mark.parametrize("use_order", [False, True])
-def test_batch_fused_matches_oracle_per_grid(sh_dtype, use_order):
+def test_batch_fused_matches_oracle_per_grid(sh_dtype, use_order, cache_samples):
+    """Without a colour cache buffer the fused batch keeps 48 samples a ray in shared memory;
+    with one of 64 samples a ray, rays longer than that gather colours again past it."""
     opt, oopt = opt_struct()
     grids, rays = _setup(sh_dtype)
-    rgbs, bufs = _batch(1, grids, rays, opt, sh_dtype, use_order, accum_for=(1,))
+    rgbs, bufs = _batch(1, grids, rays, opt, sh_dtype, use_order, accum_for=(1,), cache_samples=cache_samples)
     for (spec, og), (o, d, gt), rgb, b in zip(grids, rays, rgbs, bufs):
         ref = O.render(og, oopt, o.numpy(), d.numpy(), mode=1, rgb_gt=gt.numpy(), prec="f32")
         r64 = O.render(og, oopt, o.numpy(), d.numpy(), mode=1, rgb_gt=gt.numpy(), prec="f64", stops=ref["stops"],

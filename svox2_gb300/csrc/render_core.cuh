@@ -1648,18 +1648,25 @@ int launch_t(const GridP& g, const OptP& opt, IoP io, long long n_rays, cudaStre
   const size_t smem = sizeof(float) *
                       (size_t)warp_smem_floats(C, io.gcol != nullptr ? 0 : cap, MODE != kFwd, tile_rows<ShT, MODE>()) *
                       kWarps;
-  // per (device, colour-cache capacity): the shared-memory attribute is set on each device the
-  // kernel runs on, and the occupancy it allows is looked up once
+  // The function's dynamic shared-memory limit is one attribute per device for every
+  // configuration (colour cache in shared or global memory, its capacity), so it is only ever
+  // raised, to the largest configuration launched so far; the occupancy each configuration
+  // allows is looked up once per (device, configuration).
   static std::mutex mu;
   static std::map<std::pair<int, int>, int> blocks_per_sm;
+  static std::map<int, size_t> smem_limit;
   int dev = 0;
   SVX_CUDA_TRY(cudaGetDevice(&dev));
   int bps;
   {
     std::lock_guard<std::mutex> lk(mu);
+    size_t& lim = smem_limit[dev];
+    if (smem > lim) {
+      SVX_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      lim = smem;
+    }
     int& slot = blocks_per_sm[std::make_pair(dev, io.gcol != nullptr ? -1 : cap)];
     if (slot == 0) {
-      SVX_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       int b = 0;
       SVX_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, kThreads, smem));
       slot = b > 0 ? b : 1;

@@ -455,7 +455,10 @@ static int render_rays(const svx_grid_t* grid, const svx_rays_t* rays, const svx
     const double want = std::ceil(max_samples / 32.0) * 32.0;
     io.cap = (int)std::min(want, (double)kGlobalCapMax);
     io.gcol_warps = (long long)num_sms() * kAdjointBlocksPerSm * kWarps;
-    rc = scr.alloc(3, sizeof(float4) * (size_t)io.cap * (size_t)io.gcol_warps);
+    // with the MSI background, each slice also holds the ray's background shells (4 float4 each):
+    // int(nlayers / step) + 2 of them, as the kernel counts them
+    io.gcol_bg = grid->background_nlayers > 0 ? (int)((float)grid->background_nlayers / o.step) + 2 : 0;
+    rc = scr.alloc(3, sizeof(float4) * (size_t)(io.cap + 4 * io.gcol_bg) * (size_t)io.gcol_warps);
     if (rc) return rc;
     io.gcol = reinterpret_cast<float*>(scr.p[3]);
   }

@@ -112,8 +112,9 @@ struct IoP {
   unsigned long long* eval_count;
   unsigned long long* trace;
   int cap;         // colour cache capacity (samples per ray)
-  float* gcol;     // optional colour cache in global memory: one [cap][3] slice per resident warp
+  float* gcol;     // optional colour cache in global memory: one slice per resident warp
   long long gcol_warps;  // slices in gcol (warps of the launch)
+  int gcol_bg;     // background shells each slice also holds (4 float4 each, after the cap entries)
   // MSI background (grids that have one; render_kernel<..., BG = true>)
   const int32_t* bg_links;     // [2 reso, reso]
   const float* bg_data;        // [bg_cap, bg_nl, 4], rows 16-byte aligned
@@ -1065,13 +1066,15 @@ __device__ __forceinline__ void bg_corners(const BgArgs& b, const int l[3], long
 
 // trilerp_bg_one (render_util.cuh:155-189) of the four channels: layers, then y, then x.
 // A link past the data's rows reads as empty, like a negative one.
-__device__ __forceinline__ void bg_gather(const BgArgs& b, const int l[3], const float pos[3], float v[4]) {
+__device__ __forceinline__ void bg_gather(const BgArgs& b, const int l[3], const float pos[3], float v[4],
+                                          int lks[4]) {
   long long u[4];
   bg_corners(b, l, u);
   float c[4][4];
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     const int lk = __ldg(b.links + u[k]);
+    lks[k] = lk;
     float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), hi = lo;
     if (lk >= 0 && lk < b.cap) {
       const float4* q = reinterpret_cast<const float4*>(b.data) + (long long)lk * b.nl + l[2];
@@ -1094,31 +1097,72 @@ __device__ __forceinline__ void bg_gather(const BgArgs& b, const int l[3], const
 struct BgChunk {
   bool valid;
   int l[3];
+  int lk[4];        // the four (x, y) corners' links
   float pos[3], v[4];
   float width, pcnt, lt_before, lt_after;
   unsigned em;
   bool stopped;
 };
 
-__device__ __forceinline__ void bg_chunk(const BgArgs& b, int i0, int lane, float& invr_carry, float& lt,
-                                         BgChunk& c) {
+// The reverse pass's copy of a chunk's samples: the forward stores, per shell, the sample's
+// position in its cell and shell width, its four interpolated channels, its cell and its corner
+// links (4 float4, 64 bytes), so the reverse pass reads them instead of intersecting, mapping and
+// gathering the shell again.
+__device__ __forceinline__ void bg_store(float4* e, const BgChunk& c) {
+  e[0] = make_float4(c.pos[0], c.pos[1], c.pos[2], c.width);
+  e[1] = make_float4(c.v[0], c.v[1], c.v[2], c.v[3]);
+  e[2] = make_float4(__int_as_float(c.l[0]), __int_as_float(c.l[1]), __int_as_float(c.l[2]),
+                     __int_as_float((int)c.valid));
+  e[3] = make_float4(__int_as_float(c.lk[0]), __int_as_float(c.lk[1]), __int_as_float(c.lk[2]),
+                     __int_as_float(c.lk[3]));
+}
+
+__device__ __forceinline__ void bg_load(const float4* e, BgChunk& c) {
+  const float4 a = e[0], v = e[1], l = e[2], k = e[3];
+  c.pos[0] = a.x;
+  c.pos[1] = a.y;
+  c.pos[2] = a.z;
+  c.width = a.w;
+  c.v[0] = v.x;
+  c.v[1] = v.y;
+  c.v[2] = v.z;
+  c.v[3] = v.w;
+  c.l[0] = __float_as_int(l.x);
+  c.l[1] = __float_as_int(l.y);
+  c.l[2] = __float_as_int(l.z);
+  c.valid = __float_as_int(l.w) != 0;
+  c.lk[0] = __float_as_int(k.x);
+  c.lk[1] = __float_as_int(k.y);
+  c.lk[2] = __float_as_int(k.z);
+  c.lk[3] = __float_as_int(k.w);
+}
+
+// Locate and gather each lane's sample of the chunk and its shell width (1/r of the previous hit
+// shell minus its own, render_background_forward's invr_last).
+__device__ __forceinline__ void bg_locate(const BgArgs& b, int i0, int lane, float& invr_carry, BgChunk& c) {
   float invr = 0.f;
 #pragma unroll
   for (int j = 0; j < 3; ++j) {
     c.l[j] = 0;
     c.pos[j] = 0.f;
   }
-  c.valid = bg_sample(b, i0 + lane, invr, c.l, c.pos);
 #pragma unroll
-  for (int j = 0; j < 4; ++j) c.v[j] = 0.f;
-  if (c.valid) bg_gather(b, c.l, c.pos, c.v);
-  // 1/r of the previous hit shell (render_background_forward's invr_last)
+  for (int j = 0; j < 4; ++j) {
+    c.v[j] = 0.f;
+    c.lk[j] = -1;
+  }
+  c.valid = bg_sample(b, i0 + lane, invr, c.l, c.pos);
+  if (c.valid) bg_gather(b, c.l, c.pos, c.v, c.lk);
   const unsigned vb = __ballot_sync(kFull, c.valid);
   const unsigned below = vb & ((1u << lane) - 1u);
   const float prev = __shfl_sync(kFull, invr, below ? 31 - __clz(below) : 0);
   const float invr_last = below ? prev : invr_carry;
   if (vb) invr_carry = __shfl_sync(kFull, invr, 31 - __clz(vb));
   c.width = __fsub_rn(invr_last, invr);
+}
+
+// Transmittance through the chunk's samples with sigma > 0, from lt (updated).
+__device__ __forceinline__ void bg_transmit(const BgArgs& b, int lane, float& lt, BgChunk& c) {
   c.pcnt = __fmul_rn(__fmul_rn(c.width, b.ws), c.v[3]);
   unsigned em = __ballot_sync(kFull, c.valid && c.v[3] > 0.f);
   // Optical depth before and after each counted sample, as a prefix sum over the chunk.  The
@@ -1151,12 +1195,17 @@ __device__ __forceinline__ void bg_chunk(const BgArgs& b, int i0, int lane, floa
 
 // Background colour from log transmittance lt, brightness term included (cuvol.cu:386-476);
 // adds the number of samples that counted to *n_samples.
-__device__ __forceinline__ float3 bg_forward(const BgArgs& b, float lt, int lane, unsigned* n_samples) {
+// cache (the adjoint, when its global cache has room for the ray's shells): one 4-float4 entry per
+// shell for the reverse pass (bg_store).
+__device__ __forceinline__ float3 bg_forward(const BgArgs& b, float lt, int lane, unsigned* n_samples,
+                                             float4* cache) {
   float a0 = 0.f, a1 = 0.f, a2 = 0.f;
   float invr_carry = b.invr0;
   for (int i0 = 0; i0 < b.n_steps; i0 += 32) {
     BgChunk c;
-    bg_chunk(b, i0, lane, invr_carry, lt, c);
+    bg_locate(b, i0, lane, invr_carry, c);
+    if (cache != nullptr && i0 + lane < b.n_steps) bg_store(cache + 4 * (i0 + lane), c);
+    bg_transmit(b, lane, lt, c);
     *n_samples += __popc(c.em);
     if ((c.em >> lane) & 1u) {
       const float w = sample_weight(c.lt_before, c.pcnt);
@@ -1180,12 +1229,34 @@ __device__ __forceinline__ float3 bg_forward(const BgArgs& b, float lt, int lane
 // the background carries; each sample's share w * dot(max(colour, 0), g) comes off it in shell
 // order (a prefix sum over the chunk), and the gradients of the four channels of a corner-layer
 // row go out as one vector atomic.
+// cache: the forward's entries of this ray's shells (bg_forward), or nullptr to locate and gather
+// them again.
 __device__ __forceinline__ void bg_backward(const BgArgs& b, float lt, float g0, float g1, float g2, float accum,
-                                            float sparsity, int lane) {
+                                            float sparsity, int lane, const float4* cache) {
   float invr_carry = b.invr0;
   for (int i0 = 0; i0 < b.n_steps; i0 += 32) {
     BgChunk c;
-    bg_chunk(b, i0, lane, invr_carry, lt, c);
+    if (cache != nullptr) {
+      if (i0 + lane < b.n_steps) {
+        bg_load(cache + 4 * (i0 + lane), c);
+      } else {
+        c.valid = false;
+        c.width = 0.f;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          c.l[j] = 0;
+          c.pos[j] = 0.f;
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          c.v[j] = 0.f;
+          c.lk[j] = -1;
+        }
+      }
+    } else {
+      bg_locate(b, i0, lane, invr_carry, c);
+    }
+    bg_transmit(b, lane, lt, c);
     const bool on = (c.em >> lane) & 1u;
     const float col0 = __fadd_rn(__fmul_rn(c.v[0], kC0), 0.5f);
     const float col1 = __fadd_rn(__fmul_rn(c.v[1], kC0), 0.5f);
@@ -1212,14 +1283,12 @@ __device__ __forceinline__ void bg_backward(const BgArgs& b, float lt, float g0,
       const float gc1 = col1 > 0.f ? __fmul_rn(cw, g1) : 0.f;
       const float gc2 = col2 > 0.f ? __fmul_rn(cw, g2) : 0.f;
       // trilerp_backward_bg_one (render_util.cuh:191-232), the four channels together
-      long long u[4];
-      bg_corners(b, c.l, u);
       const float ay = __fsub_rn(1.f, c.pos[1]), ax = __fsub_rn(1.f, c.pos[0]), az = __fsub_rn(1.f, c.pos[2]);
       const float wy[4] = {ay, c.pos[1], ay, c.pos[1]};
       const float wx[4] = {ax, ax, c.pos[0], c.pos[0]};
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
-        const int lk = __ldg(b.links + u[k]);
+        const int lk = c.lk[k];
         if (lk < 0 || lk >= b.cap) continue;
         const float wk = __fmul_rn(wy[k], wx[k]);
         const float e0 = __fmul_rn(wk, gc0), e1 = __fmul_rn(wk, gc1), e2 = __fmul_rn(wk, gc2),
@@ -1263,7 +1332,10 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 5 : kAdjointBlocksPer
   const bool gown = io.gcol != nullptr && gslot < io.gcol_warps;
   // one float4 per evaluated sample: its colour (before the +0.5 offset) and the log
   // transmittance before it
-  float4* colc = reinterpret_cast<float4*>(gown ? io.gcol + gslot * io.cap * 4 : sm.col);
+  float4* colc =
+      reinterpret_cast<float4*>(gown ? io.gcol + gslot * (long long)(io.cap + 4 * io.gcol_bg) * 4 : sm.col);
+  // the MSI background's shells, after the colour entries (the adjoint's global cache only)
+  float4* bgc = gown && io.gcol_bg > 0 ? colc + io.cap : nullptr;
   const int cap = (io.gcol == nullptr || gown) ? io.cap : 0;
   const int grp = lane >> 3, cj = lane & 7;
   const long long n_rays = MULTI ? *io.n_rays_dev : io.n_rays;
@@ -1424,7 +1496,7 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 5 : kAdjointBlocksPer
       tb0 = tb1 = tb2 = bsrc.nl > 0 ? 0.f : __fmul_rn(expf(lt_fwd), opt.bg);
       if (with_bg) {
         bg_setup(bga, org, dir, g, opt, bsrc);
-        const float3 c = bg_forward(bga, lt_bg, lane, &bg_evals);
+        const float3 c = bg_forward(bga, lt_bg, lane, &bg_evals, bga.n_steps <= io.gcol_bg ? bgc : nullptr);
         tb0 = c.x;
         tb1 = c.y;
         tb2 = c.z;
@@ -1458,7 +1530,9 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 5 : kAdjointBlocksPer
       float carry;
       if constexpr (BG) {
         carry = fmaf(tb0, gout0, fmaf(tb1, gout1, __fmul_rn(tb2, gout2)));
-        if (with_bg) bg_backward(bga, lt_bg, gout0, gout1, gout2, carry, go.sparsity, lane);
+        if (with_bg)
+          bg_backward(bga, lt_bg, gout0, gout1, gout2, carry, go.sparsity, lane,
+                      bga.n_steps <= io.gcol_bg ? bgc : nullptr);
       } else {
         carry = __fmul_rn(tb, __fadd_rn(__fadd_rn(gout0, gout1), gout2));
       }

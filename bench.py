@@ -49,9 +49,11 @@ Q = 1_000_000
 BYTES_PER_SAMPLE = 3648
 BYTES_PER_RAY = 48
 # DRAM bytes (read + write) per evaluated sample of render_kernel<9, float, fused> on this
-# workload: one ncu capture (--set full) of a 131,072-ray launch read 14.920 GB and wrote
-# 5.509 GB over 20,528,014 evaluated samples; scaled to a launch by its evaluated samples.
-DRAM_BYTES_PER_SAMPLE = 995.2
+# workload: one ncu capture of a full 1M-ray launch (dram__bytes_read.sum and
+# dram__bytes_write.sum only, a single replay pass) read 49.558 GB and wrote 22.915 GB over
+# 152.66 M evaluated samples.  (A 131,072-ray launch moves 995 B per sample: fewer rays per
+# voxel, less reuse in L2.)
+DRAM_BYTES_PER_SAMPLE = 474.7
 # launches of this library per training step: ray_keys_kernel, 6 CUB radix-sort kernels,
 # render_kernel, add_accum_kernel, 2 x tv_sparse_kernel, 2 x step_mask_kernel
 LAUNCHES_PER_STEP = 13
@@ -974,8 +976,9 @@ def emit(args, rank, world, g, value, e2e_val, total_ms, kern_ms, n_eval, clk):
                 "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": DRAM_BYTES_PER_SAMPLE * n_eval / args.steps,
-                         "traffic_note": "DRAM bytes per launch, ncu capture of a 131k-ray launch scaled by "
-                                         "evaluated samples",
+                         "traffic_note": "DRAM bytes per launch: ncu capture of one full 1M-ray launch "
+                                         "(dram__bytes_read.sum + dram__bytes_write.sum), per evaluated sample "
+                                         "x this launch's evaluated samples",
                          "frac_note": "achieved counts the algorithmic bytes (every corner gathered twice, every "
                                       "gradient row read and written); corner reuse along a ray and between "
                                       "rays serves most of them from L1/L2, so it can exceed the DRAM peak. "

@@ -757,13 +757,24 @@ __device__ __forceinline__ void run_colours(int nR, bool have_prev, const WarpSm
     }
     __syncwarp();
   }
-  // shared corners, run by run (each copy reads a slot that is already complete)
+  // Shared corners, two runs per step: each copy reads a slot that is already complete.  Run q
+  // copies from run q - 1 (complete after the previous step); run q + 1 copies a corner that
+  // run q shares from where run q got it: run q's own gathered row, or run q - 1.  Two runs a
+  // step halve the chain of dependent shared-memory round trips; more runs a step cost more in
+  // instructions than they save.
   const int cj = lane >> 2, cg = lane & 3;  // 24 lanes: corner cj, group cg (< 3)
-  for (int q = 1; q <= nR; ++q) {
-    const int nd = sm.run_need[q];
-    if (cg < 3 && !((nd >> cj) & 1)) {
-      const int src = cj + sm.run_delta[q];
-      sm.slot[q * kSlotStride + cj * 3 + cg] = sm.slot[(q - 1) * kSlotStride + src * 3 + cg];
+  for (int q = 1; q <= nR; q += 2) {
+    const int nd0 = sm.run_need[q], dl0 = sm.run_delta[q];
+    const bool two = q + 1 <= nR;
+    const int nd1 = two ? sm.run_need[q + 1] : 0xFF, dl1 = two ? sm.run_delta[q + 1] : 0;
+    if (cg < 3) {
+      if (!((nd0 >> cj) & 1))
+        sm.slot[q * kSlotStride + cj * 3 + cg] = sm.slot[(q - 1) * kSlotStride + (cj + dl0) * 3 + cg];
+      if (!((nd1 >> cj) & 1)) {
+        const int j = cj + dl1;   // the corner's index in run q
+        const int src = ((nd0 >> j) & 1) ? q * kSlotStride + j * 3 : (q - 1) * kSlotStride + (j + dl0) * 3;
+        sm.slot[(q + 1) * kSlotStride + cj * 3 + cg] = sm.slot[src + cg];
+      }
     }
     __syncwarp();
   }

@@ -17,6 +17,7 @@
 
 #include <climits>
 #include <cmath>
+#include <cstdlib>
 #include <map>
 #include <mutex>
 #include <utility>
@@ -330,7 +331,7 @@ static int make_opt(const svx_render_opts_t* o, OptP* p) {
 // device's default memory pool keeps freed blocks (release threshold raised once per
 // device), so steady-state calls do not go back to the driver.
 struct Scratch {
-  void* p[4] = {nullptr, nullptr, nullptr, nullptr};
+  void* p[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   cudaStream_t st;
   explicit Scratch(cudaStream_t s) : st(s) {}
   int alloc(int i, size_t bytes) {
@@ -405,6 +406,28 @@ static int mark(const svx_render_stats_t* stats, bool stop, cudaStream_t st) {
   return SVX_OK;
 }
 
+// The fused step of an SH9 grid without the MSI background runs as two kernels, the forward
+// (kFusedFwd) and the reverse (kFusedRev), with a record per ray between them:
+// 2 + kNumCkpt + cap float4 entries (15 KB a ray at the 256^3 workload).  The records of a call
+// take at most this many bytes; larger calls run in chunks of rays, each chunk both kernels.
+// SVX_FUSED_SPLIT_BYTES sets the budget (0: always the one-kernel fused step).
+static long long split_budget_bytes() {
+  const char* e = std::getenv("SVX_FUSED_SPLIT_BYTES");
+  if (e != nullptr && *e != '\0') return std::atoll(e);
+  return 16ll << 30;
+}
+
+template <int MODE>
+static int launch_sh9(int dt, const GridP& g, const OptP& o, const IoP& io, long long n, cudaStream_t st) {
+  switch (dt) {
+    case SVX_F32: return launch_t<9, float, MODE, false, false>(g, o, io, n, st);
+    case SVX_BF16: return launch_t<9, __nv_bfloat16, MODE, false, false>(g, o, io, n, st);
+    case SVX_F16: return launch_t<9, __half, MODE, false, false>(g, o, io, n, st);
+  }
+  set_error("sh_dtype %d unknown", dt);
+  return SVX_ERR_INVALID;
+}
+
 template <int MODE>
 static int render_rays(const svx_grid_t* grid, const svx_rays_t* rays, const svx_render_opts_t* opt,
                        IoP io, const svx_render_stats_t* stats, void* stream) {
@@ -446,7 +469,19 @@ static int render_rays(const svx_grid_t* grid, const svx_rays_t* rays, const svx
   rc = scr.alloc(0, 256);
   if (rc) return rc;
   io.work = reinterpret_cast<unsigned long long*>(scr.p[0]);
-  if (MODE != kFwd) {
+  // the two-kernel fused step: every sample's colour fits the record, and the rays of a chunk
+  // are a range of the coherence order (or all of them)
+  long long split_chunk = 0, rec_stride = 0;
+  if (MODE == kFused && grid->background_nlayers == 0 && grid->basis_dim == 9) {
+    const double want = std::ceil(max_samples / 32.0) * 32.0;
+    rec_stride = 2 + kNumCkpt + (long long)want;
+    const long long budget = split_budget_bytes();
+    const long long chunk = budget / (rec_stride * (long long)sizeof(float4));
+    const bool sorted = rays->n_rays >= kSortMinRays && rays->n_rays < (1ll << 31);
+    if (want <= (double)kGlobalCapMax && chunk >= 1 && (sorted || chunk >= rays->n_rays))
+      split_chunk = std::min<long long>(chunk, rays->n_rays);
+  }
+  if (MODE != kFwd && split_chunk == 0) {
     // The adjoint's colour cache: one slice per resident warp of the launch (the adjoint
     // instantiations are bounded to kAdjointBlocksPerSm blocks per SM), as long as the grid's
     // longest ray up to kGlobalCapMax samples, 16 bytes per sample.  At the 256^3 workload that
@@ -486,8 +521,25 @@ static int render_rays(const svx_grid_t* grid, const svx_rays_t* rays, const svx
   }
   rc = mark(stats, false, st);
   if (rc) return rc;
-  rc = dispatch<MODE, false>(grid, g, o, io, rays->n_rays, st);
-  if (rc) return rc;
+  if (split_chunk > 0) {
+    io.cap = (int)(rec_stride - 2 - kNumCkpt);
+    io.rec_stride = rec_stride;
+    rc = scr.alloc(4, sizeof(float4) * (size_t)rec_stride * (size_t)split_chunk);
+    if (rc) return rc;
+    io.rec = reinterpret_cast<float4*>(scr.p[4]);
+    for (long long c0 = 0; c0 < rays->n_rays; c0 += split_chunk) {
+      IoP ioc = io;
+      ioc.n_rays = std::min(split_chunk, rays->n_rays - c0);
+      if (io.order != nullptr) ioc.order = io.order + c0;
+      rc = launch_sh9<kFusedFwd>(grid->sh_dtype, g, o, ioc, ioc.n_rays, st);
+      if (rc) return rc;
+      rc = launch_sh9<kFusedRev>(grid->sh_dtype, g, o, ioc, ioc.n_rays, st);
+      if (rc) return rc;
+    }
+  } else {
+    rc = dispatch<MODE, false>(grid, g, o, io, rays->n_rays, st);
+    if (rc) return rc;
+  }
   rc = mark(stats, true, st);
   if (rc) return rc;
   if (table) return launch_add_accum(io.accum, stride, C, grid->n_voxels, io.grad_sh, io.grad_density, st);

@@ -55,7 +55,11 @@ constexpr int kGlobalCapMax = 4096;  // global colour cache: samples per ray, at
 constexpr int kAdjointBlocksPerSm = 4;  // __launch_bounds__ of the adjoint instantiations
 constexpr long long kSortMinRays = 1 << 15;  // batches below this run in input order
 
-enum Mode { kFwd = 0, kFused = 1, kBwd = 2 };
+enum Mode { kFwd = 0, kFused = 1, kBwd = 2, kFusedFwd = 3, kFusedRev = 4 };
+// kFusedFwd / kFusedRev: the fused step as two kernels.  kFusedFwd runs the forward march and the
+// MSE residual and writes, per ray, a record: the adjoint's seed, the segment checkpoints and
+// every evaluated sample's colour and log transmittance; kFusedRev runs the reverse pass from
+// the records.  Each kernel is about half of kFused's code and fits five blocks per SM.
 
 template <typename T> struct SvxDt;
 template <> struct SvxDt<float> { static constexpr int v = SVX_F32; };
@@ -115,6 +119,8 @@ struct IoP {
   float* gcol;     // optional colour cache in global memory: one slice per resident warp
   long long gcol_warps;  // slices in gcol (warps of the launch)
   int gcol_bg;     // background shells each slice also holds (4 float4 each, after the cap entries)
+  float4* rec;     // kFusedFwd / kFusedRev: one record of rec_stride entries per ray position
+  long long rec_stride;  // 2 + kNumCkpt + cap
   // MSI background (grids that have one; render_kernel<..., BG = true>)
   const int32_t* bg_links;     // [2 reso, reso]
   const float* bg_data;        // [bg_cap, bg_nl, 4], rows 16-byte aligned
@@ -286,10 +292,11 @@ constexpr int kTileRows = 16;    // coefficient rows gathered per pass, 16-bit S
 // Coefficient rows gathered per pass.  Rows are copied into shared memory with cp.async, all rows
 // of a pass in flight at once (one memory round trip per pass, no registers held): 32 rows for
 // the adjoint instantiations, 24 for the forward-only ones, whose five blocks per SM leave less
-// shared memory per warp.
+// shared memory per warp.  The reverse kernel of the two-kernel fused step gathers no rows (its
+// colours are in the records): 0, and no row tables.
 template <typename ShT, int MODE>
 __host__ __device__ constexpr int tile_rows() {
-  return MODE == 0 ? 24 : 32;
+  return (MODE == kFwd || MODE == kFusedFwd) ? 24 : MODE == kFusedRev ? 0 : 32;
 }
 
 // 4-byte words a 16-bit row of C coefficients can span (it starts on a 2-byte boundary).
@@ -326,7 +333,7 @@ struct WarpSmem {
 // adjoint: the reverse pass's checkpoint arrays are carved (the forward-only kernel has none,
 // which lets five of its blocks share an SM).
 __host__ __device__ constexpr int warp_smem_floats(int C, int cap, bool adjoint, int rows) {
-  return (32 * 8 + 32 + kSlots * kSlotStride + tile_floats(C, rows) + 2 * kMaxRows + kSlots * 7 +
+  return (32 * 8 + 32 + kSlots * kSlotStride + tile_floats(C, rows) + 2 * (rows > 0 ? kMaxRows : 0) + kSlots * 7 +
           (adjoint ? 3 * kNumCkpt + 3 * kMaxStride : 0) + 16 + 4 * cap + 3) & ~3;
 }
 
@@ -337,8 +344,8 @@ __device__ __forceinline__ WarpSmem carve(float* base, int C, int cap, bool adjo
   s.slot = base + 32 * 8 + 32;
   s.tile = s.slot + kSlots * kSlotStride;
   s.rowlink = reinterpret_cast<int*>(s.tile + tile_floats(C, rows));
-  s.rowdst = s.rowlink + kMaxRows;
-  s.run_lane = s.rowdst + kMaxRows;
+  s.rowdst = s.rowlink + (rows > 0 ? kMaxRows : 0);
+  s.run_lane = s.rowdst + (rows > 0 ? kMaxRows : 0);
   s.run_l = s.run_lane + kSlots;
   s.run_need = s.run_l + 3 * kSlots;
   s.run_delta = s.run_need + kSlots;
@@ -1321,24 +1328,33 @@ __device__ __forceinline__ void bg_backward(const BgArgs& b, float lt, float g0,
 
 // ---------------------------------------------------------------- kernel
 
+// The adjoint modes that keep segment checkpoints in shared memory (kFusedFwd writes its own to
+// the ray's record), and the blocks per SM each mode is compiled for.
+__host__ __device__ constexpr bool ck_in_smem(int mode) { return mode == kFused || mode == kBwd || mode == kFusedRev; }
+__host__ __device__ constexpr int blocks_per_sm_bound(int mode) {
+  return (mode == kFwd || mode == kFusedFwd || mode == kFusedRev) ? 5 : kAdjointBlocksPerSm;
+}
+
 template <int BD, typename ShT, int MODE, bool IMAGE, bool MULTI, bool BG = false>
-// 128 registers and 13.8 KB of shared memory per warp (SH9, colour cache of 192 samples)
-// let four blocks (16 warps) share an SM; the march is latency-bound, so resident warps
-// count for more than the registers a larger budget would save.  The forward-only kernel
-// (no colour cache, no checkpoints: 10 KB per warp) fits five blocks at 102 registers.
-__global__ void __launch_bounds__(kThreads, MODE == kFwd ? 5 : kAdjointBlocksPerSm) render_kernel(GridP g0, OptP opt,
-                                                                                               IoP io) {
+// 128 registers and 13.8 KB of shared memory per warp (SH9) let four blocks (16 warps) of the
+// one-kernel fused step share an SM; the march is latency-bound, so resident warps count for
+// more than the registers a larger budget would save.  The forward-only kernel and the two
+// kernels of the two-kernel fused step (no colour cache in shared memory; the forward keeps no
+// checkpoints there, the reverse gathers no rows) fit five blocks at 102 registers.
+__global__ void __launch_bounds__(kThreads, blocks_per_sm_bound(MODE)) render_kernel(GridP g0, OptP opt, IoP io) {
   constexpr int C = 3 * BD;
+  constexpr bool kSplit = MODE == kFusedFwd || MODE == kFusedRev;
   extern __shared__ float4 smem4[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   // The adjoint's per-sample colour cache: a slice of io.gcol (global memory, most of it held in
   // L2 between a ray's forward and reverse passes; sized by the host for the grid's longest ray),
-  // or, without one, cap samples in shared memory.  Samples past the capacity are gathered again.
-  const int scap = io.gcol != nullptr ? 0 : io.cap;  // samples in the shared-memory cache
+  // the ray's record (two-kernel step), or, without either, cap samples in shared memory.
+  // Samples past the capacity are gathered again.
+  const int scap = (io.gcol != nullptr || kSplit) ? 0 : io.cap;  // samples in the shared-memory cache
   constexpr int TR = tile_rows<ShT, MODE>();
-  float* wbase = reinterpret_cast<float*>(smem4) + (size_t)wib * warp_smem_floats(C, scap, MODE != kFwd, TR);
-  const WarpSmem sm = carve(wbase, C, scap, MODE != kFwd, TR);
+  float* wbase = reinterpret_cast<float*>(smem4) + (size_t)wib * warp_smem_floats(C, scap, ck_in_smem(MODE), TR);
+  const WarpSmem sm = carve(wbase, C, scap, ck_in_smem(MODE), TR);
   const long long gslot = (long long)blockIdx.x * kWarps + wib;
   const bool gown = io.gcol != nullptr && gslot < io.gcol_warps;
   // one float4 per evaluated sample: its colour (before the +0.5 offset) and the log
@@ -1358,7 +1374,8 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 5 : kAdjointBlocksPer
   next = __shfl_sync(kFull, next, 0);
 
   while (next < (unsigned long long)n_rays) {
-    const long long ray = io.order != nullptr ? (long long)__ldg(io.order + next) : (long long)next;
+    const long long pos = (long long)next;   // the ray's position in the processing order
+    const long long ray = io.order != nullptr ? (long long)__ldg(io.order + pos) : pos;
     GridP g = g0;
     GridOut go{io.grad_density, io.grad_sh, io.mask, io.accum, io.accum_stride, io.norm, io.beta, io.sparsity};
     if (MULTI) load_batch_grid(io.batch_grids, __ldg(io.ray_grid + ray), g, go);
@@ -1372,6 +1389,19 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 5 : kAdjointBlocksPer
     }
     const ShT* __restrict__ sh = reinterpret_cast<const ShT*>(g.sh);
     if (lane == 0) next = atomicAdd(io.work, 1ull);  // prefetch the following ray
+    // two-kernel fused step: the ray's record (by position), its colour entries after the
+    // header (2 entries) and the checkpoints (kNumCkpt)
+    float4* rec = nullptr;
+    if constexpr (kSplit) {
+      rec = io.rec + pos * io.rec_stride;
+      colc = rec + 2 + kNumCkpt;
+    }
+    if constexpr (MODE == kFusedRev) {
+      if (__float_as_int(rec[1].x) == 0) {   // no checkpoint: no evaluated sample, no gradient
+        next = __shfl_sync(kFull, next, 0);
+        continue;
+      }
+    }
     // ---- ray setup (all lanes, redundantly)
     float org[3], dir[3];
     if (IMAGE) {
@@ -1397,11 +1427,35 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 5 : kAdjointBlocksPer
     unsigned long long th = 1469598103934665603ull;
     unsigned long long* thp = io.trace != nullptr ? &th : nullptr;
 
+    int n_eval = 0, nck = 0, stride = 1;
+    float gout0 = 0.f, gout1 = 0.f, gout2 = 0.f;   // d(loss)/d(colour) of the ray
+    float carry = 0.f;   // the adjoint's light behind the last sample
+    if constexpr (MODE == kFusedRev) {
+      // the forward kernel's record: the seed, the checkpoints
+      const float4 h0 = rec[0], h1 = rec[1];
+      gout0 = h0.x;
+      gout1 = h0.y;
+      gout2 = h0.z;
+      carry = h0.w;
+      nck = __float_as_int(h1.x);
+      stride = __float_as_int(h1.y);
+      n_eval = __float_as_int(h1.z);
+      for (int k = lane; k < nck; k += 32) {
+        const float4 c = rec[2 + k];
+        sm.ck_t[k] = c.x;
+        sm.ck_lt[k] = c.y;
+        sm.ck_idx[k] = __float_as_int(c.z);
+      }
+      __syncwarp();
+    } else {
     if (!(rg.tmin <= rg.tmax)) {
       if constexpr (!BG) {
         // Ray misses the grid: background only, no gradient (cuvol.cu:42-48, 253-258).
         if (MODE != kBwd && lane < 3) io.rgb_out[ray * 3 + lane] = opt.bg;
         if (io.trace != nullptr && lane == 0) io.trace[ray] = th;
+        if constexpr (MODE == kFusedFwd) {
+          if (lane == 0) rec[1] = make_float4(0.f, 0.f, 0.f, 0.f);   // no checkpoint
+        }
         next = __shfl_sync(kFull, next, 0);
         continue;
       }
@@ -1415,32 +1469,42 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 5 : kAdjointBlocksPer
     float acc0 = 0.f, acc1 = 0.f, acc2 = 0.f;   // this lane's samples' colour sum
     bool have_prev = false;
     long long prev_base = 0;
-    int n_eval = 0, nck = 0, stride = 1, seg_since_ck = 0;
+    int seg_since_ck = 0;
     bool stopped = false;
     while (t <= rg.tmax) {
       Seg s;
-      march_segment<MODE == kFwd>(s, t, lt, rg, g, opt, sm.links, thp, lane);
+      march_segment<MODE == kFwd || MODE == kFusedFwd>(s, t, lt, rg, g, opt, sm.links, thp, lane);
       if (s.evm) {
         if (MODE != kFwd) {
           // checkpoint the segment (thinned to every stride-th evaluated segment)
           if (seg_since_ck == 0) {
             if (nck == kNumCkpt && stride < kMaxStride) {
               // keep every other checkpoint, double the stride (kNumCkpt == 64: one per lane pair)
-              const float a = sm.ck_t[2 * lane], b = sm.ck_lt[2 * lane];
-              const int c = sm.ck_idx[2 * lane];
-              __syncwarp();
-              sm.ck_t[lane] = a;
-              sm.ck_lt[lane] = b;
-              sm.ck_idx[lane] = c;
+              if constexpr (MODE == kFusedFwd) {
+                const float4 a = rec[2 + 2 * lane];
+                __syncwarp();
+                rec[2 + lane] = a;
+              } else {
+                const float a = sm.ck_t[2 * lane], b = sm.ck_lt[2 * lane];
+                const int c = sm.ck_idx[2 * lane];
+                __syncwarp();
+                sm.ck_t[lane] = a;
+                sm.ck_lt[lane] = b;
+                sm.ck_idx[lane] = c;
+              }
               __syncwarp();
               nck = kNumCkpt / 2;
               stride *= 2;
             }
             if (nck < kNumCkpt) {  // always true within the host's samples-per-ray limit
               if (lane == 0) {
-                sm.ck_t[nck] = t;
-                sm.ck_lt[nck] = lt;
-                sm.ck_idx[nck] = n_eval;
+                if constexpr (MODE == kFusedFwd) {
+                  rec[2 + nck] = make_float4(t, lt, __int_as_float(n_eval), 0.f);
+                } else {
+                  sm.ck_t[nck] = t;
+                  sm.ck_lt[nck] = lt;
+                  sm.ck_idx[nck] = n_eval;
+                }
               }
               ++nck;
             }
@@ -1526,8 +1590,7 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 5 : kAdjointBlocksPer
 
     if (MODE != kFwd) {
       // ---- adjoint seed
-      float gout0, gout1, gout2;
-      if (MODE == kFused) {
+      if (MODE == kFused || MODE == kFusedFwd) {
         // residual of the MSE loss (cuvol.cu:735-741)
         gout0 = __fmul_rn(__fsub_rn(out0, __ldg(io.rgb_gt + ray * 3 + 0)), go.norm);
         gout1 = __fmul_rn(__fsub_rn(out1, __ldg(io.rgb_gt + ray * 3 + 1)), go.norm);
@@ -1538,7 +1601,6 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 5 : kAdjointBlocksPer
         gout2 = __ldg(io.grad_out + ray * 3 + 2);
       }
       // light that passes the last sample: background, plus the beta-loss term (cuvol.cu:259-264)
-      float carry;
       if constexpr (BG) {
         carry = fmaf(tb0, gout0, fmaf(tb1, gout1, __fmul_rn(tb2, gout2)));
         if (with_bg)
@@ -1547,12 +1609,21 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 5 : kAdjointBlocksPer
       } else {
         carry = __fmul_rn(tb, __fadd_rn(__fadd_rn(gout0, gout1), gout2));
       }
-      if (MODE == kFused && go.beta > 0.f) {
+      if ((MODE == kFused || MODE == kFusedFwd) && go.beta > 0.f) {
         const float tin = expf(lt_fwd);
         const double f = 1.0 - (double)tin / __dadd_rn((double)__fsub_rn(1.f, tin), 1e-3);
         carry = __fadd_rn(carry, (float)((double)go.beta * f));
       }
+      if constexpr (MODE == kFusedFwd) {
+        if (lane == 0) {   // the record's header; the checkpoints are written as they are made
+          rec[0] = make_float4(gout0, gout1, gout2, carry);
+          rec[1] = make_float4(__int_as_float(nck), __int_as_float(stride), __int_as_float(n_eval), 0.f);
+        }
+      }
+    }
+    }   // the forward (all modes but kFusedRev)
 
+    if constexpr (MODE == kFused || MODE == kBwd || MODE == kFusedRev) {
       // ---- reverse pass over checkpointed segments
       float B = 0.f;               // lanes <24: colour gradient per (g, corner); 24..31: density
       int lk_lane = -1;            // link of corner (lane & 7) of the tracked cell
@@ -1595,7 +1666,7 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 5 : kAdjointBlocksPer
           const float t0 = sm.tmp_t[b], lt0 = sm.tmp_lt[b];
           const int idx0 = sm.tmp_idx[b];
           // segments the colour cache holds replay the forward's transmittance
-          const bool cached = idx0 + 32 <= cap;
+          const bool cached = kSplit || idx0 + 32 <= cap;
           march_segment(s, t0, lt0, rg, g, opt, sm.links, nullptr, lane, cached ? colc : nullptr, idx0, n_eval);
           __syncwarp();
           int slot;
@@ -1605,7 +1676,7 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 5 : kAdjointBlocksPer
           float col[3] = {0.f, 0.f, 0.f};
           float w8[8];
           corner_weights(s.pos[0], s.pos[1], s.pos[2], w8);
-          if (idx0 + __popc(s.evm) <= cap) {
+          if (kSplit || idx0 + __popc(s.evm) <= cap) {
             if (ev) {
               const float4 e = colc[idx0 + rank];
               col[0] = e.x;
@@ -1613,9 +1684,11 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 5 : kAdjointBlocksPer
               col[2] = e.z;
             }
           } else {
-            // colours past the cache: gather again
-            run_colours<BD, ShT, TR>(nR, false, sm, basis, sh, lane);
-            if (ev) lane_colour(sm, slot, w8, col);
+            // colours past the cache: gather again (the two-kernel step's records hold them all)
+            if constexpr (TR > 0) {
+              run_colours<BD, ShT, TR>(nR, false, sm, basis, sh, lane);
+              if (ev) lane_colour(sm, slot, w8, col);
+            }
           }
           // d(loss)/d(colour) pieces, trace_ray_cuvol_backward cuvol.cu:311-344
           const float w = ev ? sample_weight(s.lt_before, s.pcnt) : 0.f;
@@ -1731,7 +1804,8 @@ int launch_t(const GridP& g, const OptP& opt, IoP io, long long n_rays, cudaStre
   io.cap = cap;
   if (MODE == kFwd) io.gcol = nullptr;
   const size_t smem = sizeof(float) *
-                      (size_t)warp_smem_floats(C, io.gcol != nullptr ? 0 : cap, MODE != kFwd, tile_rows<ShT, MODE>()) *
+                      (size_t)warp_smem_floats(C, (io.gcol != nullptr || MODE == kFusedFwd || MODE == kFusedRev) ? 0 : cap,
+                                               ck_in_smem(MODE), tile_rows<ShT, MODE>()) *
                       kWarps;
   // The function's dynamic shared-memory limit is one attribute per device for every
   // configuration (colour cache in shared or global memory, its capacity), so it is only ever

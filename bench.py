@@ -48,15 +48,16 @@ N_BALLS = 8
 Q = 1_000_000
 BYTES_PER_SAMPLE = 3648
 BYTES_PER_RAY = 48
-# DRAM bytes (read + write) per evaluated sample of render_kernel<9, float, fused> on this
-# workload: one ncu capture of a full 1M-ray launch (dram__bytes_read.sum and
-# dram__bytes_write.sum only, a single replay pass) read 49.558 GB and wrote 22.915 GB over
-# 152.66 M evaluated samples.  (A 131,072-ray launch moves 995 B per sample: fewer rays per
-# voxel, less reuse in L2.)
-DRAM_BYTES_PER_SAMPLE = 474.7
+# DRAM bytes (read + write) per evaluated sample of the fused step on this workload (its two
+# kernels, render_kernel<9, float, kFusedFwd> and <9, float, kFusedRev>): one ncu capture of
+# three full 1M-ray steps (dram__bytes_read.sum and dram__bytes_write.sum only, a single replay
+# pass per launch) measured 22.00 GB (forward) + 29.88 GB (reverse) per step over 155.83 M
+# evaluated samples per step.
+DRAM_BYTES_PER_SAMPLE = 332.9
 # launches of this library per training step: ray_keys_kernel, 6 CUB radix-sort kernels,
-# render_kernel, add_accum_kernel, 2 x tv_sparse_kernel, 2 x step_mask_kernel
-LAUNCHES_PER_STEP = 13
+# render_kernel twice (the fused step's forward and reverse kernels), add_accum_kernel,
+# 2 x tv_sparse_kernel, 2 x step_mask_kernel
+LAUNCHES_PER_STEP = 14
 METRIC = "fused fwd+bwd rays/s at 256^3 SH9 (train step: render+MSE adjoint, TV, RMSprop)"
 WORKLOAD = "train step 256^3 20% occupancy SH9 FP32, 1M rays/step, fused fwd+bwd + TV + RMSprop"
 
@@ -976,9 +977,9 @@ def emit(args, rank, world, g, value, e2e_val, total_ms, kern_ms, n_eval, clk):
                 "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": DRAM_BYTES_PER_SAMPLE * n_eval / args.steps,
-                         "traffic_note": "DRAM bytes per launch: ncu capture of one full 1M-ray launch "
-                                         "(dram__bytes_read.sum + dram__bytes_write.sum), per evaluated sample "
-                                         "x this launch's evaluated samples",
+                         "traffic_note": "DRAM bytes per step of the fused step's two kernels: ncu capture "
+                                         "of full 1M-ray steps (dram__bytes_read.sum + dram__bytes_write.sum), "
+                                         "per evaluated sample x this step's evaluated samples",
                          "frac_note": "achieved counts the algorithmic bytes (every corner gathered twice, every "
                                       "gradient row read and written); corner reuse along a ray and between "
                                       "rays serves most of them from L1/L2, so it can exceed the DRAM peak. "
@@ -986,7 +987,8 @@ def emit(args, rank, world, g, value, e2e_val, total_ms, kern_ms, n_eval, clk):
                          "dram_achieved": DRAM_BYTES_PER_SAMPLE * n_eval / args.steps / per_launch_s / 1e9,
                          "dram_frac": DRAM_BYTES_PER_SAMPLE * n_eval / args.steps / per_launch_s / 1e9 / peak,
                          "peak_kind": peak_kind,
-                         "kernel": "render_kernel<9,float,fused> (ray march + MSE adjoint)",
+                         "kernel": "the fused step: render_kernel<9,float,kFusedFwd> (forward march, MSE "
+                                   "residual, per-ray records) + render_kernel<9,float,kFusedRev> (adjoint)",
                          "kernel_ms": kern_ms / args.steps, "eval_samples_per_step": n_eval / args.steps,
                          "algorithmic_bytes_per_launch": alg_bytes},
             "cpu_baseline": cpu,

@@ -469,10 +469,12 @@ static int render_rays(const svx_grid_t* grid, const svx_rays_t* rays, const svx
   rc = scr.alloc(0, 256);
   if (rc) return rc;
   io.work = reinterpret_cast<unsigned long long*>(scr.p[0]);
-  // the two-kernel fused step: every sample's colour fits the record, and the rays of a chunk
-  // are a range of the coherence order (or all of them)
+  // the two-kernel form of the fused step and of the plain backward (the latter without the MSI
+  // background, whose adjoint there starts from the backward pass's own transmittance): every
+  // sample's colour fits the record, and the rays of a chunk are a range of the coherence order
+  // (or all of them)
   long long split_chunk = 0, rec_stride = 0;
-  if (MODE == kFused && grid->background_nlayers == 0 && grid->basis_dim == 9) {
+  if (grid->basis_dim == 9 && (MODE == kFused || (MODE == kBwd && grid->background_nlayers == 0))) {
     const double want = std::ceil(max_samples / 32.0) * 32.0;
     rec_stride = 2 + kNumCkpt + (long long)want;
     const long long budget = split_budget_bytes();
@@ -480,6 +482,15 @@ static int render_rays(const svx_grid_t* grid, const svx_rays_t* rays, const svx
     const bool sorted = rays->n_rays >= kSortMinRays && rays->n_rays < (1ll << 31);
     if (want <= (double)kGlobalCapMax && chunk >= 1 && (sorted || chunk >= rays->n_rays))
       split_chunk = std::min<long long>(chunk, rays->n_rays);
+  }
+  if (split_chunk > 0 && grid->background_nlayers > 0) {
+    // the forward kernel's MSI background passes keep their shells in a per-warp slice, as in
+    // the one-kernel step (int(nlayers / step) + 2 shells, 4 float4 each)
+    io.gcol_warps = (long long)num_sms() * blocks_per_sm_bound(kFusedFwd) * kWarps;
+    io.gcol_bg = (int)((float)grid->background_nlayers / o.step) + 2;
+    rc = scr.alloc(3, sizeof(float4) * 4 * (size_t)io.gcol_bg * (size_t)io.gcol_warps);
+    if (rc) return rc;
+    io.gcol = reinterpret_cast<float*>(scr.p[3]);
   }
   if (MODE != kFwd && split_chunk == 0) {
     // The adjoint's colour cache: one slice per resident warp of the launch (the adjoint
@@ -531,7 +542,8 @@ static int render_rays(const svx_grid_t* grid, const svx_rays_t* rays, const svx
       IoP ioc = io;
       ioc.n_rays = std::min(split_chunk, rays->n_rays - c0);
       if (io.order != nullptr) ioc.order = io.order + c0;
-      rc = launch_sh9<kFusedFwd>(grid->sh_dtype, g, o, ioc, ioc.n_rays, st);
+      rc = grid->background_nlayers > 0 ? launch_bg_split_fwd(grid->sh_dtype, g, o, ioc, ioc.n_rays, st)
+                                        : launch_sh9<kFusedFwd>(grid->sh_dtype, g, o, ioc, ioc.n_rays, st);
       if (rc) return rc;
       rc = launch_sh9<kFusedRev>(grid->sh_dtype, g, o, ioc, ioc.n_rays, st);
       if (rc) return rc;

@@ -56,10 +56,12 @@ constexpr int kAdjointBlocksPerSm = 4;  // __launch_bounds__ of the adjoint inst
 constexpr long long kSortMinRays = 1 << 15;  // batches below this run in input order
 
 enum Mode { kFwd = 0, kFused = 1, kBwd = 2, kFusedFwd = 3, kFusedRev = 4 };
-// kFusedFwd / kFusedRev: the fused step as two kernels.  kFusedFwd runs the forward march and the
-// MSE residual and writes, per ray, a record: the adjoint's seed, the segment checkpoints and
-// every evaluated sample's colour and log transmittance; kFusedRev runs the reverse pass from
-// the records.  Each kernel is about half of kFused's code and fits five blocks per SM.
+// kFusedFwd / kFusedRev: the fused step (or the plain backward) as two kernels.  kFusedFwd runs
+// the forward march and the adjoint's seed (the MSE residual, or the given grad_out; with the MSI
+// background also the background's forward and adjoint) and writes, per ray, a record: the seed,
+// the segment checkpoints and every evaluated sample's colour and log transmittance; kFusedRev
+// runs the foreground's reverse pass from the records.  Each kernel is about half of kFused's
+// code and fits five blocks per SM.
 
 template <typename T> struct SvxDt;
 template <> struct SvxDt<float> { static constexpr int v = SVX_F32; };
@@ -1359,11 +1361,13 @@ __global__ void __launch_bounds__(kThreads, blocks_per_sm_bound(MODE)) render_ke
   const bool gown = io.gcol != nullptr && gslot < io.gcol_warps;
   // one float4 per evaluated sample: its colour (before the +0.5 offset) and the log
   // transmittance before it
-  float4* colc =
-      reinterpret_cast<float4*>(gown ? io.gcol + gslot * (long long)(io.cap + 4 * io.gcol_bg) * 4 : sm.col);
+  // (in the two-kernel step the colours go to the ray's record and the slice holds only the
+  // MSI background's shells)
+  const long long slice = kSplit ? 4ll * io.gcol_bg : (long long)io.cap + 4ll * io.gcol_bg;
+  float4* colc = gown ? reinterpret_cast<float4*>(io.gcol) + gslot * slice : reinterpret_cast<float4*>(sm.col);
   // the MSI background's shells, after the colour entries (the adjoint's global cache only)
-  float4* bgc = gown && io.gcol_bg > 0 ? colc + io.cap : nullptr;
-  const int cap = (io.gcol == nullptr || gown) ? io.cap : 0;
+  float4* bgc = gown && io.gcol_bg > 0 ? (kSplit ? colc : colc + io.cap) : nullptr;
+  const int cap = (kSplit || io.gcol == nullptr || gown) ? io.cap : 0;
   const int grp = lane >> 3, cj = lane & 7;
   const long long n_rays = MULTI ? *io.n_rays_dev : io.n_rays;
 
@@ -1451,7 +1455,7 @@ __global__ void __launch_bounds__(kThreads, blocks_per_sm_bound(MODE)) render_ke
     if (!(rg.tmin <= rg.tmax)) {
       if constexpr (!BG) {
         // Ray misses the grid: background only, no gradient (cuvol.cu:42-48, 253-258).
-        if (MODE != kBwd && lane < 3) io.rgb_out[ray * 3 + lane] = opt.bg;
+        if (MODE != kBwd && io.rgb_out != nullptr && lane < 3) io.rgb_out[ray * 3 + lane] = opt.bg;
         if (io.trace != nullptr && lane == 0) io.trace[ray] = th;
         if constexpr (MODE == kFusedFwd) {
           if (lane == 0) rec[1] = make_float4(0.f, 0.f, 0.f, 0.f);   // no checkpoint
@@ -1581,7 +1585,7 @@ __global__ void __launch_bounds__(kThreads, blocks_per_sm_bound(MODE)) render_ke
     }
     const float tb = tb0;
     const float out0 = __fadd_rn(acc0, tb0), out1 = __fadd_rn(acc1, tb1), out2 = __fadd_rn(acc2, tb2);
-    if (MODE != kBwd && lane == 0) {
+    if (MODE != kBwd && io.rgb_out != nullptr && lane == 0) {
       io.rgb_out[ray * 3 + 0] = out0;
       io.rgb_out[ray * 3 + 1] = out1;
       io.rgb_out[ray * 3 + 2] = out2;
@@ -1590,7 +1594,8 @@ __global__ void __launch_bounds__(kThreads, blocks_per_sm_bound(MODE)) render_ke
 
     if (MODE != kFwd) {
       // ---- adjoint seed
-      if (MODE == kFused || MODE == kFusedFwd) {
+      // kFusedFwd serves both the fused step (the residual) and the plain backward (given grad_out)
+      if (MODE == kFused || (MODE == kFusedFwd && io.grad_out == nullptr)) {
         // residual of the MSE loss (cuvol.cu:735-741)
         gout0 = __fmul_rn(__fsub_rn(out0, __ldg(io.rgb_gt + ray * 3 + 0)), go.norm);
         gout1 = __fmul_rn(__fsub_rn(out1, __ldg(io.rgb_gt + ray * 3 + 1)), go.norm);
@@ -1857,6 +1862,9 @@ int dispatch_bd(int bd, int dt, const GridP& g, const OptP& opt, const IoP& io, 
 // Launches the render kernel of a grid with the MSI background (render_bg.cu).
 int dispatch_bg(int mode, bool image, int bd, int dt, const GridP& g, const OptP& opt, const IoP& io,
                 long long n, cudaStream_t st);
+// Launches the forward kernel of the two-kernel fused step (SH9) for a grid with the MSI
+// background (render_bg.cu); its reverse kernel is the one without the background.
+int launch_bg_split_fwd(int dt, const GridP& g, const OptP& opt, const IoP& io, long long n, cudaStream_t st);
 // Launches the batch kernel (SH9) whose grids may have an MSI background (render_bg.cu).
 int dispatch_bg_batch(int mode, int dt, const GridP& g, const OptP& opt, const IoP& io, long long n,
                       cudaStream_t st);

@@ -1,15 +1,18 @@
-"""The fused step as two kernels (forward with per-ray records, then the reverse pass from them).
+"""The fused step and the plain backward as two kernels (a forward with per-ray records, then
+the reverse pass from them).
 
-svx_volume_render_cuvol_fused runs an SH9 grid without the MSI background as two kernels when
-the per-ray records fit the budget (SVX_FUSED_SPLIT_BYTES, read at each call), in chunks of
-rays when they do not all fit at once, and as the one-kernel fused step when the budget is 0.
-Every GPU fused test runs the two-kernel form at its default budget; this file holds the three
-forms to one another and to the oracle on the same inputs:
+For SH9 grids, svx_volume_render_cuvol_fused (with or without the MSI background) and
+svx_volume_render_cuvol_backward (without it) run as two kernels when the per-ray records fit
+the budget (SVX_FUSED_SPLIT_BYTES, read at each call), in chunks of rays when they do not all fit
+at once, and as one kernel when the budget is 0.  Every GPU test of those entries runs the
+two-kernel form at its default budget; this file holds the forms to one another and to the
+oracle on the same inputs:
   * colours and the per-ray sample trace bit for bit between the forms (the forward arithmetic is
     the same; only the gradient atomics' order differs);
-  * gradients and masks of each form against the oracle (helpers.check_fused);
+  * gradients and masks of each form against the oracle (helpers.check_fused, assert_grad_f64);
   * an unsorted small batch, a coherence-sorted batch with the accumulation rows, several chunks,
-    BF16 storage, last_sample_opaque and the beta / sparsity terms.
+    BF16 storage, last_sample_opaque and the beta / sparsity terms; the plain backward; the MSI
+    background (forms against each other).
 """
 import os
 
@@ -79,3 +82,106 @@ def test_two_kernel_fused_matches_one_kernel_and_oracle(name):
     for label, (rgb, grads, st) in (("two kernels", two), ("one kernel", one)):
         check_fused(rgb, grads, st["ray_trace"].cpu().numpy(), st["eval_samples"].item(), og, oopt, o, d, gt,
                     beta=beta, sparsity=sparsity, label=f"{name} {label}")
+
+
+def _bwd(budget, spec, rays, opt, go, N, n_sh):
+    from svox2_gb300 import csrc as C
+    grads = C.GridOutputGrads()
+    grads.grad_density_out = torch.zeros((N, 1), device="cuda")
+    grads.grad_sh_out = torch.zeros((N, n_sh), device="cuda")
+    old = os.environ.get(ENV)
+    try:
+        if budget is None:
+            os.environ.pop(ENV, None)
+        else:
+            os.environ[ENV] = str(budget)
+        C.volume_render_cuvol_backward(spec, rays, opt, go, None, grads)
+        torch.cuda.synchronize()
+    finally:
+        if old is None:
+            os.environ.pop(ENV, None)
+        else:
+            os.environ[ENV] = old
+    return grads
+
+
+@pytest.mark.parametrize("Q", [1024, 40960])
+def test_two_kernel_backward_matches_one_kernel_and_oracle(Q):
+    """The plain backward (given dL/dcolour) in both forms against the float64 oracle."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from helpers import assert_grad_f64
+    import oracle.oracle as O
+    grid = S.make_grid(40, occupancy=0.3, seed=63)
+    spec, og = grid_pair(grid)
+    o, d, _ = S.make_rays(Q, seed=64)
+    rays = rays_pair(o, d)
+    opt, oopt = opt_struct()
+    go = torch.randn((Q, 3), generator=torch.Generator().manual_seed(65))
+    N, n_sh = og.density.shape[0], og.sh.shape[1]
+    ref = O.render(og, oopt, o.numpy(), d.numpy(), mode=0, trace=False)
+    rb = O.render(og, oopt, o.numpy(), d.numpy(), mode=2, grad_out=go.numpy(), color=ref["rgb"], prec="f64",
+                  stops=ref["stops"], want_magnitude=True)
+    two = _bwd(None, spec, rays, opt, go.cuda(), N, n_sh)
+    one = _bwd(0, spec, rays, opt, go.cuda(), N, n_sh)
+    for label, gr in (("two kernels", two), ("one kernel", one)):
+        assert_grad_f64(gr.grad_density_out.cpu().numpy(), rb["grad_density"], rb["mag_density"],
+                        f"{Q} {label} grad_density")
+        assert_grad_f64(gr.grad_sh_out.cpu().numpy(), rb["grad_sh"], rb["mag_sh"], f"{Q} {label} grad_sh")
+
+
+@pytest.mark.parametrize("Q", [2000, 40960])
+def test_two_kernel_background_matches_one_kernel(Q):
+    """With the MSI background the forward kernel also runs the background's adjoint; both forms
+    on the same inputs: colours bit for bit, masks equal, gradients within 1e-5 of the largest
+    entry (only the atomics' order differs).  The background tests hold the default form to
+    the oracle and to the reference's kernels."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from svox2_gb300 import csrc as C
+    grid = S.make_grid(24, occupancy=0.3, seed=66)
+    spec, og = grid_pair(grid)
+    gen = torch.Generator().manual_seed(67)
+    keep = torch.rand((32, 16), generator=gen) >= 0.2
+    links = torch.full(keep.shape, -1, dtype=torch.int32)
+    links[keep] = torch.arange(int(keep.sum()), dtype=torch.int32)
+    data = torch.randn((int(keep.sum()), 8, 4), generator=gen) * 0.5
+    data[..., 3] = torch.rand((int(keep.sum()), 8), generator=gen) * 4.0 - 0.5
+    spec.background_links, spec.background_data = links.cuda(), data.cuda()
+    o, d, gt = S.make_rays(Q, seed=68)
+    dr = torch.randn((Q // 2, 3), generator=gen)
+    d[Q // 2:] = dr / dr.norm(dim=-1, keepdim=True)
+    rays = rays_pair(o, d.contiguous())
+    opt, _ = opt_struct()
+    N, n_sh = og.density.shape[0], og.sh.shape[1]
+    out = {}
+    for budget in (None, 0):
+        old = os.environ.get(ENV)
+        try:
+            if budget is None:
+                os.environ.pop(ENV, None)
+            else:
+                os.environ[ENV] = str(budget)
+            rgb = torch.zeros((Q, 3), device="cuda")
+            grads = C.GridOutputGrads()
+            grads.grad_density_out = torch.zeros((N, 1), device="cuda")
+            grads.grad_sh_out = torch.zeros((N, n_sh), device="cuda")
+            grads.mask_out = torch.zeros((N,), dtype=torch.bool, device="cuda")
+            grads.grad_background_out = torch.zeros(tuple(data.shape), device="cuda")
+            grads.mask_background_out = torch.zeros(tuple(data.shape[:2]), dtype=torch.bool, device="cuda")
+            C.volume_render_cuvol_fused(spec, rays, opt, gt.cuda(), 0.0, 0.0, rgb, grads)
+            torch.cuda.synchronize()
+            out[budget] = (rgb, grads)
+        finally:
+            if old is None:
+                os.environ.pop(ENV, None)
+            else:
+                os.environ[ENV] = old
+    (r2, g2), (r1, g1) = out[None], out[0]
+    np.testing.assert_array_equal(r2.cpu().numpy(), r1.cpu().numpy())
+    for key in ("mask_out", "mask_background_out"):
+        np.testing.assert_array_equal(getattr(g2, key).cpu().numpy(), getattr(g1, key).cpu().numpy())
+    for key in ("grad_density_out", "grad_sh_out", "grad_background_out"):
+        a, b = getattr(g2, key).cpu().numpy().astype(np.float64), getattr(g1, key).cpu().numpy()
+        err = np.abs(a - b).max() / max(np.abs(b).max(), 1e-30)
+        assert err <= 1e-5, f"{Q} {key}: two-kernel vs one-kernel {err:.2e}"

@@ -335,21 +335,38 @@ struct Scratch {
   cudaStream_t st;
   explicit Scratch(cudaStream_t s) : st(s) {}
   int alloc(int i, size_t bytes) {
+    const int rc = tune_pool();
+    if (rc) return rc;
+    SVX_CUDA_TRY(cudaMallocAsync(&p[i], bytes, st));
+    return SVX_OK;
+  }
+  // As alloc, but a pool that cannot supply the bytes is not an error: returns -1, with the CUDA
+  // error state cleared, so the caller can take a path that needs less memory.
+  int try_alloc(int i, size_t bytes) {
+    const int rc = tune_pool();
+    if (rc) return rc;
+    const cudaError_t e = cudaMallocAsync(&p[i], bytes, st);
+    if (e == cudaErrorMemoryAllocation) {
+      (void)cudaGetLastError();
+      p[i] = nullptr;
+      return -1;
+    }
+    SVX_CUDA_TRY(e);
+    return SVX_OK;
+  }
+  static int tune_pool() {
     static std::mutex mu;
     static bool tuned[64] = {false};
     int dev = 0;
     SVX_CUDA_TRY(cudaGetDevice(&dev));
-    {
-      std::lock_guard<std::mutex> lk(mu);
-      if (dev >= 0 && dev < 64 && !tuned[dev]) {
-        cudaMemPool_t pool;
-        SVX_CUDA_TRY(cudaDeviceGetDefaultMemPool(&pool, dev));
-        uint64_t thr = ~0ull;
-        SVX_CUDA_TRY(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
-        tuned[dev] = true;
-      }
+    std::lock_guard<std::mutex> lk(mu);
+    if (dev >= 0 && dev < 64 && !tuned[dev]) {
+      cudaMemPool_t pool;
+      SVX_CUDA_TRY(cudaDeviceGetDefaultMemPool(&pool, dev));
+      uint64_t thr = ~0ull;
+      SVX_CUDA_TRY(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+      tuned[dev] = true;
     }
-    SVX_CUDA_TRY(cudaMallocAsync(&p[i], bytes, st));
     return SVX_OK;
   }
   ~Scratch() {
@@ -482,6 +499,15 @@ static int render_rays(const svx_grid_t* grid, const svx_rays_t* rays, const svx
     const bool sorted = rays->n_rays >= kSortMinRays && rays->n_rays < (1ll << 31);
     if (want <= (double)kGlobalCapMax && chunk >= 1 && (sorted || chunk >= rays->n_rays))
       split_chunk = std::min<long long>(chunk, rays->n_rays);
+    if (split_chunk > 0) {
+      // the records; a device that cannot hold them runs the one-kernel step instead
+      rc = scr.try_alloc(4, sizeof(float4) * (size_t)rec_stride * (size_t)split_chunk);
+      if (rc == -1) {
+        split_chunk = 0;
+        rc = SVX_OK;
+      }
+      if (rc) return rc;
+    }
   }
   if (split_chunk > 0 && grid->background_nlayers > 0) {
     // the forward kernel's MSI background passes keep their shells in a per-warp slice, as in
@@ -535,8 +561,6 @@ static int render_rays(const svx_grid_t* grid, const svx_rays_t* rays, const svx
   if (split_chunk > 0) {
     io.cap = (int)(rec_stride - 2 - kNumCkpt);
     io.rec_stride = rec_stride;
-    rc = scr.alloc(4, sizeof(float4) * (size_t)rec_stride * (size_t)split_chunk);
-    if (rc) return rc;
     io.rec = reinterpret_cast<float4*>(scr.p[4]);
     for (long long c0 = 0; c0 < rays->n_rays; c0 += split_chunk) {
       IoP ioc = io;

@@ -423,15 +423,17 @@ static int mark(const svx_render_stats_t* stats, bool stop, cudaStream_t st) {
   return SVX_OK;
 }
 
-// The fused step of an SH9 grid without the MSI background runs as two kernels, the forward
-// (kFusedFwd) and the reverse (kFusedRev), with a record per ray between them:
-// 2 + kNumCkpt + cap float4 entries (15 KB a ray at the 256^3 workload).  The records of a call
-// take at most this many bytes; larger calls run in chunks of rays, each chunk both kernels.
-// SVX_FUSED_SPLIT_BYTES sets the budget (0: always the one-kernel fused step).
+// The fused step of an SH9 grid runs as two kernels, the forward (kFusedFwd) and the reverse
+// (kFusedRev), with a record per ray between them: 2 + cap float4 entries and cap float2 ones
+// (cap = the grid's longest ray in samples, rounded up to 32; 21.5 KB a ray at the 256^3
+// workload).  The records of a call
+// take at most this many bytes (default 24 GiB: a million rays of the 256^3 workload in one
+// chunk); larger calls run in chunks of rays, each chunk both kernels.  SVX_FUSED_SPLIT_BYTES sets
+// the budget (0: always the one-kernel fused step).
 static long long split_budget_bytes() {
   const char* e = std::getenv("SVX_FUSED_SPLIT_BYTES");
   if (e != nullptr && *e != '\0') return std::atoll(e);
-  return 16ll << 30;
+  return 24ll << 30;
 }
 
 template <int MODE>
@@ -493,7 +495,7 @@ static int render_rays(const svx_grid_t* grid, const svx_rays_t* rays, const svx
   long long split_chunk = 0, rec_stride = 0;
   if (grid->basis_dim == 9 && (MODE == kFused || (MODE == kBwd && grid->background_nlayers == 0))) {
     const double want = std::ceil(max_samples / 32.0) * 32.0;
-    rec_stride = 2 + kNumCkpt + (long long)want;
+    rec_stride = 2 + (long long)want + (long long)want / 2;
     const long long budget = split_budget_bytes();
     const long long chunk = budget / (rec_stride * (long long)sizeof(float4));
     const bool sorted = rays->n_rays >= kSortMinRays && rays->n_rays < (1ll << 31);
@@ -559,7 +561,7 @@ static int render_rays(const svx_grid_t* grid, const svx_rays_t* rays, const svx
   rc = mark(stats, false, st);
   if (rc) return rc;
   if (split_chunk > 0) {
-    io.cap = (int)(rec_stride - 2 - kNumCkpt);
+    io.cap = (int)((rec_stride - 2) / 3 * 2);
     io.rec_stride = rec_stride;
     io.rec = reinterpret_cast<float4*>(scr.p[4]);
     for (long long c0 = 0; c0 < rays->n_rays; c0 += split_chunk) {

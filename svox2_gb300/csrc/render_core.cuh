@@ -58,10 +58,10 @@ constexpr long long kSortMinRays = 1 << 15;  // batches below this run in input 
 enum Mode { kFwd = 0, kFused = 1, kBwd = 2, kFusedFwd = 3, kFusedRev = 4 };
 // kFusedFwd / kFusedRev: the fused step (or the plain backward) as two kernels.  kFusedFwd runs
 // the forward march and the adjoint's seed (the MSE residual, or the given grad_out; with the MSI
-// background also the background's forward and adjoint) and writes, per ray, a record: the seed,
-// the segment checkpoints and every evaluated sample's colour and log transmittance; kFusedRev
-// runs the foreground's reverse pass from the records.  Each kernel is about half of kFused's
-// code and fits five blocks per SM.
+// background also the background's forward and adjoint) and writes, per ray, a record: the seed
+// and, for every evaluated sample, its colour, the log transmittance before it, its t and sigma;
+// kFusedRev runs the foreground's reverse pass from the records, without marching again.  Each
+// kernel is about half of kFused's code and fits five or six blocks per SM.
 
 template <typename T> struct SvxDt;
 template <> struct SvxDt<float> { static constexpr int v = SVX_F32; };
@@ -122,7 +122,7 @@ struct IoP {
   long long gcol_warps;  // slices in gcol (warps of the launch)
   int gcol_bg;     // background shells each slice also holds (4 float4 each, after the cap entries)
   float4* rec;     // kFusedFwd / kFusedRev: one record of rec_stride entries per ray position
-  long long rec_stride;  // 2 + kNumCkpt + cap
+  long long rec_stride;  // 2 + cap + cap / 2 (header, colour entries, (t, sigma) pairs)
   // MSI background (grids that have one; render_kernel<..., BG = true>)
   const int32_t* bg_links;     // [2 reso, reso]
   const float* bg_data;        // [bg_cap, bg_nl, 4], rows 16-byte aligned
@@ -581,6 +581,55 @@ __device__ __forceinline__ void march_segment(Seg& s, float t0, float lt0, const
     s.t_next = __fadd_rn(__shfl_sync(kFull, tk, 31), opt.step);
     s.end = !(s.t_next <= r.tmax) || !(s.t_next > t0);
   }
+}
+
+// The reverse kernel of the two-kernel step reads its samples from the ray's record instead of
+// marching again: evaluated samples c0 .. c0 + 31 (those below n_eval), each with the t and sigma
+// and the log transmittance before it that the forward kernel stored.  From t it forms the grid
+// position, cell and corner weights with the forward's operations, and loads the cell's corner
+// links (for the gradient flush); sigma needs no density gathers.  Fills the fields of Seg the
+// adjoint reads; evm holds the lanes with a sample.
+__device__ __forceinline__ void record_chunk(Seg& s, const float4* ent, const float2* tsig, int c0, int n_eval,
+                                             const RayGeo& r, const GridP& g, const OptP& opt, int* slinks,
+                                             int lane) {
+  __syncwarp();  // every lane is done with the previous chunk's staged links
+  const int idx = c0 + lane;
+  const bool valid = idx < n_eval;
+  float tk = 0.f, sigma = 0.f, ltb = 0.f;
+  if (valid) {
+    const float2 a = tsig[idx];
+    tk = a.x;
+    sigma = a.y;
+    ltb = ent[idx].w;
+  }
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    float p = fmaf(tk, r.d[j], r.o[j]);
+    p = fminf(fmaxf(p, 0.f), (float)g.size[j] - 1.f);
+    s.l[j] = min((int)p, g.size[j] - 2);
+    s.pos[j] = __fsub_rn(p, (float)s.l[j]);
+  }
+  const long long base = (long long)s.l[0] * g.offx + (long long)s.l[1] * g.offy + s.l[2];
+  s.base = base;
+  if (valid) {
+    const int32_t* lp = g.links + base;
+    int4* dst = reinterpret_cast<int4*>(slinks + lane * 8);
+    dst[0] = make_int4(__ldg(lp), __ldg(lp + 1), __ldg(lp + g.offy), __ldg(lp + g.offy + 1));
+    dst[1] = make_int4(__ldg(lp + g.offx), __ldg(lp + g.offx + 1), __ldg(lp + g.offx + g.offy),
+                       __ldg(lp + g.offx + g.offy + 1));
+  }
+  s.t = tk;
+  s.sigma = sigma;
+  s.ws = (opt.last_opaque && __fadd_rn(tk, opt.step) > r.tmax) ? 1e9f : r.world_step;
+  s.pcnt = __fmul_rn(s.ws, sigma);
+  s.lt_before = ltb;
+  s.lt_after = valid ? __fsub_rn(ltb, s.pcnt) : 0.f;
+  s.evm = __ballot_sync(kFull, valid);
+  s.n = __popc(s.evm);
+  s.stopped = false;
+  s.end = true;
+  s.t_next = 0.f;
+  s.lt_end = 0.f;
 }
 
 // Weight of a sample: T * (1 - exp(-sigma * step)) (trace_ray_cuvol, cuvol.cu:92).  The
@@ -1330,10 +1379,11 @@ __device__ __forceinline__ void bg_backward(const BgArgs& b, float lt, float g0,
 
 // ---------------------------------------------------------------- kernel
 
-// The adjoint modes that keep segment checkpoints in shared memory (kFusedFwd writes its own to
-// the ray's record), and the blocks per SM each mode is compiled for.  The reverse kernel of the
+// The adjoint modes that keep segment checkpoints in shared memory (the two-kernel step needs
+// none: its reverse kernel reads every evaluated sample from the record), and the blocks per SM
+// each mode is compiled for.  The reverse kernel of the
 // two-kernel step fits six (80 registers, 48 bytes spilled: 2% faster than five at 96).
-__host__ __device__ constexpr bool ck_in_smem(int mode) { return mode == kFused || mode == kBwd || mode == kFusedRev; }
+__host__ __device__ constexpr bool ck_in_smem(int mode) { return mode == kFused || mode == kBwd; }
 __host__ __device__ constexpr int blocks_per_sm_bound(int mode) {
   return mode == kFusedRev ? 6 : (mode == kFwd || mode == kFusedFwd) ? 5 : kAdjointBlocksPerSm;
 }
@@ -1394,15 +1444,18 @@ __global__ void __launch_bounds__(kThreads, blocks_per_sm_bound(MODE)) render_ke
     }
     const ShT* __restrict__ sh = reinterpret_cast<const ShT*>(g.sh);
     if (lane == 0) next = atomicAdd(io.work, 1ull);  // prefetch the following ray
-    // two-kernel fused step: the ray's record (by position), its colour entries after the
-    // header (2 entries) and the checkpoints (kNumCkpt)
+    // two-kernel fused step: the ray's record (by position): a header of 2 entries, the colour
+    // entries (cap float4: colour, log transmittance before the sample), then cap float2 (t,
+    // sigma) of the evaluated samples
     float4* rec = nullptr;
+    float2* tsig_out = nullptr;
     if constexpr (kSplit) {
       rec = io.rec + pos * io.rec_stride;
-      colc = rec + 2 + kNumCkpt;
+      colc = rec + 2;
+      tsig_out = reinterpret_cast<float2*>(rec + 2 + cap);
     }
     if constexpr (MODE == kFusedRev) {
-      if (__float_as_int(rec[1].x) == 0) {   // no checkpoint: no evaluated sample, no gradient
+      if (__float_as_int(rec[1].x) == 0) {   // no evaluated sample: no gradient
         next = __shfl_sync(kFull, next, 0);
         continue;
       }
@@ -1436,22 +1489,13 @@ __global__ void __launch_bounds__(kThreads, blocks_per_sm_bound(MODE)) render_ke
     float gout0 = 0.f, gout1 = 0.f, gout2 = 0.f;   // d(loss)/d(colour) of the ray
     float carry = 0.f;   // the adjoint's light behind the last sample
     if constexpr (MODE == kFusedRev) {
-      // the forward kernel's record: the seed, the checkpoints
-      const float4 h0 = rec[0], h1 = rec[1];
+      // the forward kernel's record: the seed and the evaluated-sample count
+      const float4 h0 = rec[0];
       gout0 = h0.x;
       gout1 = h0.y;
       gout2 = h0.z;
       carry = h0.w;
-      nck = __float_as_int(h1.x);
-      stride = __float_as_int(h1.y);
-      n_eval = __float_as_int(h1.z);
-      for (int k = lane; k < nck; k += 32) {
-        const float4 c = rec[2 + k];
-        sm.ck_t[k] = c.x;
-        sm.ck_lt[k] = c.y;
-        sm.ck_idx[k] = __float_as_int(c.z);
-      }
-      __syncwarp();
+      n_eval = __float_as_int(rec[1].x);
     } else {
     if (!(rg.tmin <= rg.tmax)) {
       if constexpr (!BG) {
@@ -1459,7 +1503,7 @@ __global__ void __launch_bounds__(kThreads, blocks_per_sm_bound(MODE)) render_ke
         if (MODE != kBwd && io.rgb_out != nullptr && lane < 3) io.rgb_out[ray * 3 + lane] = opt.bg;
         if (io.trace != nullptr && lane == 0) io.trace[ray] = th;
         if constexpr (MODE == kFusedFwd) {
-          if (lane == 0) rec[1] = make_float4(0.f, 0.f, 0.f, 0.f);   // no checkpoint
+          if (lane == 0) rec[1] = make_float4(0.f, 0.f, 0.f, 0.f);   // no evaluated sample
         }
         next = __shfl_sync(kFull, next, 0);
         continue;
@@ -1480,36 +1524,26 @@ __global__ void __launch_bounds__(kThreads, blocks_per_sm_bound(MODE)) render_ke
       Seg s;
       march_segment<MODE == kFwd || MODE == kFusedFwd>(s, t, lt, rg, g, opt, sm.links, thp, lane);
       if (s.evm) {
-        if (MODE != kFwd) {
+        if (MODE != kFwd && MODE != kFusedFwd) {
           // checkpoint the segment (thinned to every stride-th evaluated segment)
           if (seg_since_ck == 0) {
             if (nck == kNumCkpt && stride < kMaxStride) {
               // keep every other checkpoint, double the stride (kNumCkpt == 64: one per lane pair)
-              if constexpr (MODE == kFusedFwd) {
-                const float4 a = rec[2 + 2 * lane];
-                __syncwarp();
-                rec[2 + lane] = a;
-              } else {
-                const float a = sm.ck_t[2 * lane], b = sm.ck_lt[2 * lane];
-                const int c = sm.ck_idx[2 * lane];
-                __syncwarp();
-                sm.ck_t[lane] = a;
-                sm.ck_lt[lane] = b;
-                sm.ck_idx[lane] = c;
-              }
+              const float a = sm.ck_t[2 * lane], b = sm.ck_lt[2 * lane];
+              const int c = sm.ck_idx[2 * lane];
+              __syncwarp();
+              sm.ck_t[lane] = a;
+              sm.ck_lt[lane] = b;
+              sm.ck_idx[lane] = c;
               __syncwarp();
               nck = kNumCkpt / 2;
               stride *= 2;
             }
             if (nck < kNumCkpt) {  // always true within the host's samples-per-ray limit
               if (lane == 0) {
-                if constexpr (MODE == kFusedFwd) {
-                  rec[2 + nck] = make_float4(t, lt, __int_as_float(n_eval), 0.f);
-                } else {
-                  sm.ck_t[nck] = t;
-                  sm.ck_lt[nck] = lt;
-                  sm.ck_idx[nck] = n_eval;
-                }
+                sm.ck_t[nck] = t;
+                sm.ck_lt[nck] = lt;
+                sm.ck_idx[nck] = n_eval;
               }
               ++nck;
             }
@@ -1530,7 +1564,10 @@ __global__ void __launch_bounds__(kThreads, blocks_per_sm_bound(MODE)) render_ke
           acc2 = fmaf(w, fmaxf(__fadd_rn(col[2], 0.5f), 0.f), acc2);
           if (MODE != kFwd) {
             const int idx = n_eval + __popc(s.evm & ((1u << lane) - 1u));
-            if (idx < cap) colc[idx] = make_float4(col[0], col[1], col[2], s.lt_before);
+            if (idx < cap) {
+              colc[idx] = make_float4(col[0], col[1], col[2], s.lt_before);
+              if constexpr (MODE == kFusedFwd) tsig_out[idx] = make_float2(s.t, s.sigma);
+            }
           }
         }
         // carry the last run to the next segment (after every lane has read the slots)
@@ -1621,9 +1658,9 @@ __global__ void __launch_bounds__(kThreads, blocks_per_sm_bound(MODE)) render_ke
         carry = __fadd_rn(carry, (float)((double)go.beta * f));
       }
       if constexpr (MODE == kFusedFwd) {
-        if (lane == 0) {   // the record's header; the checkpoints are written as they are made
+        if (lane == 0) {   // the record's header
           rec[0] = make_float4(gout0, gout1, gout2, carry);
-          rec[1] = make_float4(__int_as_float(nck), __int_as_float(stride), __int_as_float(n_eval), 0.f);
+          rec[1] = make_float4(__int_as_float(n_eval), 0.f, 0.f, 0.f);
         }
       }
     }
@@ -1635,148 +1672,163 @@ __global__ void __launch_bounds__(kThreads, blocks_per_sm_bound(MODE)) render_ke
       int lk_lane = -1;            // link of corner (lane & 7) of the tracked cell
       int bcell[3] = {0, 0, 0};
       bool have_b = false;
-      for (int k = nck - 1; k >= 0; --k) {
-        // starts of the evaluated segments this checkpoint covers
-        int cnt = 0;
-        if (stride == 1) {
-          if (lane == 0) {
-            sm.tmp_t[0] = sm.ck_t[k];
-            sm.tmp_lt[0] = sm.ck_lt[k];
-            sm.tmp_idx[0] = sm.ck_idx[k];
-          }
-          cnt = 1;
-          __syncwarp();
-        } else {
-          float tt = sm.ck_t[k], ll = sm.ck_lt[k];
-          int ii = sm.ck_idx[k];
-          while (cnt < stride) {
-            Seg s;
-            march_segment(s, tt, ll, rg, g, opt, sm.links, nullptr, lane);
-            if (s.evm) {
-              if (lane == 0) {
-                sm.tmp_t[cnt] = tt;
-                sm.tmp_lt[cnt] = ll;
-                sm.tmp_idx[cnt] = ii;
-              }
-              ++cnt;
-              ii += __popc(s.evm);
-            }
-            ll = s.lt_end;
-            if (s.stopped || s.end) break;
-            tt = s.t_next;
-          }
-          __syncwarp();
-        }
-        for (int b = cnt - 1; b >= 0; --b) {
-          Seg s;
-          const float t0 = sm.tmp_t[b], lt0 = sm.tmp_lt[b];
-          const int idx0 = sm.tmp_idx[b];
-          // segments the colour cache holds replay the forward's transmittance
-          const bool cached = kSplit || idx0 + 32 <= cap;
-          march_segment(s, t0, lt0, rg, g, opt, sm.links, nullptr, lane, cached ? colc : nullptr, idx0, n_eval);
-          __syncwarp();
-          int slot;
-          const int nR = segment_runs(s, false, 0, sm, lane, &slot);
-          const bool ev = (s.evm >> lane) & 1u;
-          const int rank = __popc(s.evm & ((1u << lane) - 1u));
-          float col[3] = {0.f, 0.f, 0.f};
-          float w8[8];
-          corner_weights(s.pos[0], s.pos[1], s.pos[2], w8);
-          if (kSplit || idx0 + __popc(s.evm) <= cap) {
-            if (ev) {
-              const float4 e = colc[idx0 + rank];
-              col[0] = e.x;
-              col[1] = e.y;
-              col[2] = e.z;
-            }
-          } else {
-            // colours past the cache: gather again (the two-kernel step's records hold them all)
-            if constexpr (TR > 0) {
-              run_colours<BD, ShT, TR>(nR, false, sm, basis, sh, lane);
-              if (ev) lane_colour(sm, slot, w8, col);
-            }
-          }
-          // d(loss)/d(colour) pieces, trace_ray_cuvol_backward cuvol.cu:311-344
-          const float w = ev ? sample_weight(s.lt_before, s.pcnt) : 0.f;
-          const float tn = expf(s.lt_after);
-          const float sc0 = __fadd_rn(col[0], 0.5f), sc1 = __fadd_rn(col[1], 0.5f), sc2 = __fadd_rn(col[2], 0.5f);
-          const float tc = __fadd_rn(__fadd_rn(__fmul_rn(fmaxf(sc0, 0.f), gout0), __fmul_rn(fmaxf(sc2, 0.f), gout2)),
-                                     __fmul_rn(fmaxf(sc1, 0.f), gout1));
-          // light after each sample = carry + suffix sum of w * tc over the later samples
-          const float v = ev ? __fmul_rn(w, tc) : 0.f;
-          float incl = v;
-#pragma unroll
-          for (int d = 1; d < 32; d <<= 1) {
-            const float y = __shfl_down_sync(kFull, incl, d);
-            if (lane + d < 32) incl = __fadd_rn(incl, y);
-          }
-          float excl = __shfl_down_sync(kFull, incl, 1);
-          if (lane == 31) excl = 0.f;
-          const float after = __fadd_rn(carry, excl);
-          float gsig = __fmul_rn(s.ws, __fsub_rn(__fmul_rn(tc, tn), after));
-          if (go.sparsity > 0.f) {
-            const float sg = s.sigma;
-            gsig = fmaf(go.sparsity, __fdiv_rn(__fmul_rn(4.f, sg), __fadd_rn(1.f, __fmul_rn(2.f, __fmul_rn(sg, sg)))),
-                        gsig);
-          }
-          carry = __fadd_rn(carry, __shfl_sync(kFull, incl, 0));
-          const float a0 = sc0 >= 0.f ? __fmul_rn(w, gout0) : 0.f;
-          const float a1 = sc1 >= 0.f ? __fmul_rn(w, gout1) : 0.f;
-          const float a2 = sc2 >= 0.f ? __fmul_rn(w, gout2) : 0.f;
-          // accumulate per run: slot[r][g*8 + j] (g = 3: density)
-          __syncwarp();  // colours read from the slots (re-gather path) are consumed
-          for (int q = lane; q < (nR + 1) * kSlotStride; q += 32) sm.slot[q] = 0.f;
-          __syncwarp();
+      // the adjoint of one segment's evaluated samples (s), whose cache entries start at idx0
+      auto adjoint_segment = [&](Seg& s, int idx0) {
+        int slot;
+        const int nR = segment_runs(s, false, 0, sm, lane, &slot);
+        const bool ev = (s.evm >> lane) & 1u;
+        const int rank = __popc(s.evm & ((1u << lane) - 1u));
+        float col[3] = {0.f, 0.f, 0.f};
+        float w8[8];
+        corner_weights(s.pos[0], s.pos[1], s.pos[2], w8);
+        if (kSplit || idx0 + __popc(s.evm) <= cap) {
           if (ev) {
-            float* d = sm.slot + slot * kSlotStride;
+            const float4 e = colc[idx0 + rank];
+            col[0] = e.x;
+            col[1] = e.y;
+            col[2] = e.z;
+          }
+        } else {
+          // colours past the cache: gather again (the two-kernel step's records hold them all)
+          if constexpr (TR > 0) {
+            run_colours<BD, ShT, TR>(nR, false, sm, basis, sh, lane);
+            if (ev) lane_colour(sm, slot, w8, col);
+          }
+        }
+        // d(loss)/d(colour) pieces, trace_ray_cuvol_backward cuvol.cu:311-344
+        const float w = ev ? sample_weight(s.lt_before, s.pcnt) : 0.f;
+        const float tn = expf(s.lt_after);
+        const float sc0 = __fadd_rn(col[0], 0.5f), sc1 = __fadd_rn(col[1], 0.5f), sc2 = __fadd_rn(col[2], 0.5f);
+        const float tc = __fadd_rn(__fadd_rn(__fmul_rn(fmaxf(sc0, 0.f), gout0), __fmul_rn(fmaxf(sc2, 0.f), gout2)),
+                                   __fmul_rn(fmaxf(sc1, 0.f), gout1));
+        // light after each sample = carry + suffix sum of w * tc over the later samples
+        const float v = ev ? __fmul_rn(w, tc) : 0.f;
+        float incl = v;
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
-              atomicAdd(d + 0 * 8 + j, __fmul_rn(w8[j], a0));
-              atomicAdd(d + 1 * 8 + j, __fmul_rn(w8[j], a1));
-              atomicAdd(d + 2 * 8 + j, __fmul_rn(w8[j], a2));
-              atomicAdd(d + 3 * 8 + j, __fmul_rn(w8[j], gsig));
-            }
+        for (int d = 1; d < 32; d <<= 1) {
+          const float y = __shfl_down_sync(kFull, incl, d);
+          if (lane + d < 32) incl = __fadd_rn(incl, y);
+        }
+        float excl = __shfl_down_sync(kFull, incl, 1);
+        if (lane == 31) excl = 0.f;
+        const float after = __fadd_rn(carry, excl);
+        float gsig = __fmul_rn(s.ws, __fsub_rn(__fmul_rn(tc, tn), after));
+        if (go.sparsity > 0.f) {
+          const float sg = s.sigma;
+          gsig = fmaf(go.sparsity, __fdiv_rn(__fmul_rn(4.f, sg), __fadd_rn(1.f, __fmul_rn(2.f, __fmul_rn(sg, sg)))),
+                      gsig);
+        }
+        carry = __fadd_rn(carry, __shfl_sync(kFull, incl, 0));
+        const float a0 = sc0 >= 0.f ? __fmul_rn(w, gout0) : 0.f;
+        const float a1 = sc1 >= 0.f ? __fmul_rn(w, gout1) : 0.f;
+        const float a2 = sc2 >= 0.f ? __fmul_rn(w, gout2) : 0.f;
+        // accumulate per run: slot[r][g*8 + j] (g = 3: density)
+        __syncwarp();  // colours read from the slots (re-gather path) are consumed
+        for (int q = lane; q < (nR + 1) * kSlotStride; q += 32) sm.slot[q] = 0.f;
+        __syncwarp();
+        if (ev) {
+          float* d = sm.slot + slot * kSlotStride;
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            atomicAdd(d + 0 * 8 + j, __fmul_rn(w8[j], a0));
+            atomicAdd(d + 1 * 8 + j, __fmul_rn(w8[j], a1));
+            atomicAdd(d + 2 * 8 + j, __fmul_rn(w8[j], a2));
+            atomicAdd(d + 3 * 8 + j, __fmul_rn(w8[j], gsig));
           }
-          __syncwarp();
-          // walk the runs last to first: merge shared corners, list the others, flush the list
-          float* fl_val = sm.tile;
-          int* fl_link = reinterpret_cast<int*>(sm.tile + kFlushCap * 4);
-          int F = 0;
-          walk_info(nR, have_b, bcell, sm, lane);
-          for (int q = nR; q >= 1; --q) {
-            const int info = sm.run_walk[q];
-            if (info & kWalkTrans) {
-              // old corners not shared with the new cell (those on the faces it moved across) retire
-              const unsigned retire = (unsigned)info & 0xFFu;
-              if (retire) {
-                if (F + 8 > kFlushCap) {
-                  if (go.accum != nullptr)
-                    flush_list_vec<BD>(F, fl_val, fl_link, sm.basis, go.accum, go.accum_stride, go.mask, lane);
-                  else
-                    flush_list<BD>(F, fl_val, fl_link, my_basis, go.grad_sh, go.grad_density, go.mask, lane);
-                  F = 0;
-                }
-                list_retiring(retire, B, lk_lane, fl_val, fl_link, F, lane);
-                F += __popc(retire);
+        }
+        __syncwarp();
+        // walk the runs last to first: merge shared corners, list the others, flush the list
+        float* fl_val = sm.tile;
+        int* fl_link = reinterpret_cast<int*>(sm.tile + kFlushCap * 4);
+        int F = 0;
+        walk_info(nR, have_b, bcell, sm, lane);
+        for (int q = nR; q >= 1; --q) {
+          const int info = sm.run_walk[q];
+          if (info & kWalkTrans) {
+            // old corners not shared with the new cell (those on the faces it moved across) retire
+            const unsigned retire = (unsigned)info & 0xFFu;
+            if (retire) {
+              if (F + 8 > kFlushCap) {
+                if (go.accum != nullptr)
+                  flush_list_vec<BD>(F, fl_val, fl_link, sm.basis, go.accum, go.accum_stride, go.mask, lane);
+                else
+                  flush_list<BD>(F, fl_val, fl_link, my_basis, go.grad_sh, go.grad_density, go.mask, lane);
+                F = 0;
               }
-              const bool fresh = (info >> (8 + cj)) & 1;
-              const int delta = ((info >> 16) & 31) - 16;
-              const float moved = __shfl_sync(kFull, B, fresh ? lane : lane + delta);
-              B = fresh ? 0.f : moved;
-              lk_lane = sm.links[sm.run_lane[q] * 8 + cj];
+              list_retiring(retire, B, lk_lane, fl_val, fl_link, F, lane);
+              F += __popc(retire);
             }
-            B = __fadd_rn(B, sm.slot[q * kSlotStride + lane]);
+            const bool fresh = (info >> (8 + cj)) & 1;
+            const int delta = ((info >> 16) & 31) - 16;
+            const float moved = __shfl_sync(kFull, B, fresh ? lane : lane + delta);
+            B = fresh ? 0.f : moved;
+            lk_lane = sm.links[sm.run_lane[q] * 8 + cj];
           }
-          if (nR > 0) {
-            bcell[0] = sm.run_l[3];
-            bcell[1] = sm.run_l[4];
-            bcell[2] = sm.run_l[5];
-            have_b = true;
+          B = __fadd_rn(B, sm.slot[q * kSlotStride + lane]);
+        }
+        if (nR > 0) {
+          bcell[0] = sm.run_l[3];
+          bcell[1] = sm.run_l[4];
+          bcell[2] = sm.run_l[5];
+          have_b = true;
+        }
+        if (go.accum != nullptr)
+          flush_list_vec<BD>(F, fl_val, fl_link, sm.basis, go.accum, go.accum_stride, go.mask, lane);
+        else
+          flush_list<BD>(F, fl_val, fl_link, my_basis, go.grad_sh, go.grad_density, go.mask, lane);
+      };
+      if constexpr (MODE == kFusedRev) {
+        // the ray's evaluated samples, last chunk of 32 first, from the record
+        const float4* ent = rec + 2;
+        const float2* tsig = reinterpret_cast<const float2*>(rec + 2 + cap);
+        for (int c0 = ((n_eval - 1) >> 5) << 5; c0 >= 0; c0 -= 32) {
+          Seg s;
+          record_chunk(s, ent, tsig, c0, n_eval, rg, g, opt, sm.links, lane);
+          adjoint_segment(s, c0);
+        }
+      } else {
+        for (int k = nck - 1; k >= 0; --k) {
+          // starts of the evaluated segments this checkpoint covers
+          int cnt = 0;
+          if (stride == 1) {
+            if (lane == 0) {
+              sm.tmp_t[0] = sm.ck_t[k];
+              sm.tmp_lt[0] = sm.ck_lt[k];
+              sm.tmp_idx[0] = sm.ck_idx[k];
+            }
+            cnt = 1;
+            __syncwarp();
+          } else {
+            float tt = sm.ck_t[k], ll = sm.ck_lt[k];
+            int ii = sm.ck_idx[k];
+            while (cnt < stride) {
+              Seg s;
+              march_segment(s, tt, ll, rg, g, opt, sm.links, nullptr, lane);
+              if (s.evm) {
+                if (lane == 0) {
+                  sm.tmp_t[cnt] = tt;
+                  sm.tmp_lt[cnt] = ll;
+                  sm.tmp_idx[cnt] = ii;
+                }
+                ++cnt;
+                ii += __popc(s.evm);
+              }
+              ll = s.lt_end;
+              if (s.stopped || s.end) break;
+              tt = s.t_next;
+            }
+            __syncwarp();
           }
-          if (go.accum != nullptr)
-            flush_list_vec<BD>(F, fl_val, fl_link, sm.basis, go.accum, go.accum_stride, go.mask, lane);
-          else
-            flush_list<BD>(F, fl_val, fl_link, my_basis, go.grad_sh, go.grad_density, go.mask, lane);
+          for (int b = cnt - 1; b >= 0; --b) {
+            Seg s;
+            const float t0 = sm.tmp_t[b], lt0 = sm.tmp_lt[b];
+            const int idx0 = sm.tmp_idx[b];
+            // segments the colour cache holds replay the forward's transmittance
+            const bool cached = idx0 + 32 <= cap;
+            march_segment(s, t0, lt0, rg, g, opt, sm.links, nullptr, lane, cached ? colc : nullptr, idx0, n_eval);
+            __syncwarp();
+            adjoint_segment(s, idx0);
+          }
         }
       }
       if (have_b) {

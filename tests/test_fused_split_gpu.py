@@ -45,9 +45,10 @@ def _run(budget, spec, rays, opt, gt, N, n_sh, **kw):
 
 
 def _record_bytes(reso, step=0.5):
-    # 2 + 64 + ceil(max samples / 32) * 32 float4 entries per ray, as the host sizes them
+    # 2 + cap float4 and cap float2 entries per ray, cap = ceil(max samples / 32) * 32, as the
+    # host sizes them
     cap = int(np.ceil((np.sqrt(3.0) * reso / step + 2.0) / 32.0) * 32)
-    return 16 * (2 + 64 + cap)
+    return 16 * (2 + cap + cap // 2)
 
 
 CASES = {

@@ -178,12 +178,12 @@ int svx_volume_render_cuvol_backward(const svx_grid_t* grid, const svx_rays_t* r
  * Renders rgb_out [n_rays,3] and accumulates the gradient of
  * mean((rgb_out - rgb_gt)^2) (+ beta_loss, sparsity_loss terms) into grads,
  * setting grads->mask_out for every touched voxel.
- * Scratch comes from the device's default stream-ordered pool.  For an SH9 grid without the
- * MSI background the step runs as two kernels with a record per ray between them
- * (16 * (66 + cap) bytes, cap = the grid's longest ray in samples rounded up to 32: 15.4 KB a
- * ray at 256^3, step 0.5); the records of one call take at most SVX_FUSED_SPLIT_BYTES bytes
- * (environment variable, read at each call; default 16 GiB), larger calls run in chunks of rays,
- * and 0 selects the one-kernel form. */
+ * Scratch comes from the device's default stream-ordered pool.  For an SH9 grid the step runs
+ * as two kernels with a record per ray between them (24 * cap + 32 bytes, cap = the grid's
+ * longest ray in samples rounded up to 32: 21.5 KB a ray at 256^3, step 0.5); the records of one
+ * call take at most SVX_FUSED_SPLIT_BYTES bytes (environment variable, read at each call;
+ * default 24 GiB), larger calls run in chunks of rays, 0 selects the one-kernel form, and so does
+ * a pool that cannot supply the records. */
 int svx_volume_render_cuvol_fused(const svx_grid_t* grid, const svx_rays_t* rays,
                                   const svx_render_opts_t* opt, const float* rgb_gt,
                                   float beta_loss, float sparsity_loss, float* rgb_out,

@@ -514,7 +514,7 @@ static int render_rays(const svx_grid_t* grid, const svx_rays_t* rays, const svx
   if (split_chunk > 0 && grid->background_nlayers > 0) {
     // the forward kernel's MSI background passes keep their shells in a per-warp slice, as in
     // the one-kernel step (int(nlayers / step) + 2 shells, 4 float4 each)
-    io.gcol_warps = (long long)num_sms() * blocks_per_sm_bound(kFusedFwd) * kWarps;
+    io.gcol_warps = (long long)num_sms() * blocks_per_sm_bound(kFusedFwd, false, true) * kWarps;
     io.gcol_bg = (int)((float)grid->background_nlayers / o.step) + 2;
     rc = scr.alloc(3, sizeof(float4) * 4 * (size_t)io.gcol_bg * (size_t)io.gcol_warps);
     if (rc) return rc;

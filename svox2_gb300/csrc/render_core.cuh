@@ -61,7 +61,7 @@ enum Mode { kFwd = 0, kFused = 1, kBwd = 2, kFusedFwd = 3, kFusedRev = 4 };
 // background also the background's forward and adjoint) and writes, per ray, a record: the seed
 // and, for every evaluated sample, its colour, the log transmittance before it, its t and sigma;
 // kFusedRev runs the foreground's reverse pass from the records, without marching again.  Each
-// kernel is about half of kFused's code and fits five or six blocks per SM.
+// kernel is about half of kFused's code and fits six blocks per SM.
 
 template <typename T> struct SvxDt;
 template <> struct SvxDt<float> { static constexpr int v = SVX_F32; };
@@ -289,12 +289,18 @@ static __device__ __noinline__ float skip_dist(int32_t link, int l0, int l1, int
 // slots 1..32 hold this segment's runs.
 constexpr int kSlots = 33;
 constexpr int kSlotStride = 33;  // floats per slot (odd: lanes reading different slots hit different banks)
-constexpr int kTileRows = 16;    // coefficient rows gathered per pass, 16-bit SH (loads through registers)
+
+// Floats per slot by mode: the forward kernels keep 24 colour values a slot (8 corners x 3
+// groups), the adjoint 32 gradient sums (4 groups x 8 corners); both strides are odd, so lanes
+// reading different slots hit different banks.  The forward kernels also carve no run-walk
+// array: with these, their shared memory fits six blocks per SM.
+__host__ __device__ constexpr int slot_stride(int mode) { return (mode == kFwd || mode == kFusedFwd) ? 25 : kSlotStride; }
+__host__ __device__ constexpr bool has_walk(int mode) { return !(mode == kFwd || mode == kFusedFwd); }
 
 // Coefficient rows gathered per pass.  Rows are copied into shared memory with cp.async, all rows
 // of a pass in flight at once (one memory round trip per pass, no registers held): 32 rows for
-// the adjoint instantiations, 24 for the forward-only ones, whose five blocks per SM leave less
-// shared memory per warp.  The reverse kernel of the two-kernel fused step gathers no rows (its
+// the adjoint instantiations, 24 for the forward ones, whose six blocks per SM leave less shared
+// memory per warp.  The reverse kernel of the two-kernel fused step gathers no rows (its
 // colours are in the records): 0, and no row tables.
 template <typename ShT, int MODE>
 __host__ __device__ constexpr int tile_rows() {
@@ -312,15 +318,16 @@ __host__ __device__ constexpr int tile_floats(int C, int rows) {
 
 struct WarpSmem {
   int* links;        // [32][8] corner links of the staged samples
-  float* slot;       // [kSlots][kSlotStride]: D[j*3+g] (colour pass) or B[g*8+j] (adjoint)
+  float* slot;       // [kSlots][slot stride]: D[j*3+g] (colour pass) or B[g*8+j] (adjoint)
   float* tile;       // [rows][C] gathered coefficient rows; in the adjoint, the flush list
   int* rowlink;      // [kMaxRows] link of each row to gather
-  int* rowdst;       // [kMaxRows] slot*8 + corner of each row
+  short* rowdst;     // [kMaxRows] slot*8 + corner of each row
   int* run_lane;     // [kSlots] first lane of each run
   int* run_l;        // [kSlots][3] cell of each run
   int* run_need;     // [kSlots] corners the run gathers (bit mask)
   int* run_delta;    // [kSlots] index offset of a shared corner in the previous run
   int* run_walk;     // [kSlots] adjoint: each run's transition from the run after it (walk_info)
+                     // (none in the forward kernels)
   float* pc;         // [32] forward-only march: the segment's optical depths (0 where not evaluated)
   float* ck_t;       // [kNumCkpt]
   float* ck_lt;      // [kNumCkpt]
@@ -333,26 +340,27 @@ struct WarpSmem {
 };
 
 // adjoint: the reverse pass's checkpoint arrays are carved (the forward-only kernel has none,
-// which lets five of its blocks share an SM).
-__host__ __device__ constexpr int warp_smem_floats(int C, int cap, bool adjoint, int rows) {
-  return (32 * 8 + 32 + kSlots * kSlotStride + tile_floats(C, rows) + 2 * (rows > 0 ? kMaxRows : 0) + kSlots * 7 +
-          (adjoint ? 3 * kNumCkpt + 3 * kMaxStride : 0) + 16 + 4 * cap + 3) & ~3;
+// which lets five of its blocks share an SM).  ss: floats per slot; walk: the run-walk array.
+__host__ __device__ constexpr int warp_smem_floats(int C, int cap, bool adjoint, int rows, int ss, bool walk) {
+  return (32 * 8 + 32 + kSlots * ss + tile_floats(C, rows) + (rows > 0 ? kMaxRows + kMaxRows / 2 : 0) +
+          kSlots * (walk ? 7 : 6) + (adjoint ? 3 * kNumCkpt + 3 * kMaxStride : 0) + 16 + 4 * cap + 3) & ~3;
 }
 
-__device__ __forceinline__ WarpSmem carve(float* base, int C, int cap, bool adjoint, int rows) {
+__device__ __forceinline__ WarpSmem carve(float* base, int C, int cap, bool adjoint, int rows, int ss, bool walk) {
   WarpSmem s;
+  const int nrow = rows > 0 ? kMaxRows : 0;
   s.links = reinterpret_cast<int*>(base);
   s.pc = base + 32 * 8;
   s.slot = base + 32 * 8 + 32;
-  s.tile = s.slot + kSlots * kSlotStride;
+  s.tile = s.slot + kSlots * ss;
   s.rowlink = reinterpret_cast<int*>(s.tile + tile_floats(C, rows));
-  s.rowdst = s.rowlink + (rows > 0 ? kMaxRows : 0);
-  s.run_lane = s.rowdst + (rows > 0 ? kMaxRows : 0);
+  s.rowdst = reinterpret_cast<short*>(s.rowlink + nrow);
+  s.run_lane = s.rowlink + nrow + nrow / 2;
   s.run_l = s.run_lane + kSlots;
   s.run_need = s.run_l + 3 * kSlots;
   s.run_delta = s.run_need + kSlots;
-  s.run_walk = s.run_delta + kSlots;
-  s.ck_t = reinterpret_cast<float*>(s.run_walk + kSlots);
+  s.run_walk = walk ? s.run_delta + kSlots : nullptr;
+  s.ck_t = reinterpret_cast<float*>(s.run_delta + kSlots + (walk ? kSlots : 0));
   s.ck_lt = s.ck_t + kNumCkpt;
   s.ck_idx = reinterpret_cast<int*>(s.ck_lt + kNumCkpt);
   s.tmp_t = reinterpret_cast<float*>(s.ck_idx + kNumCkpt);
@@ -706,7 +714,7 @@ __device__ __forceinline__ void cp_async4(float* dst, const float* src, int src_
 
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-template <int BD, typename ShT, int TR>
+template <int BD, typename ShT, int TR, int SS>
 __device__ __forceinline__ void run_colours(int nR, bool have_prev, const WarpSmem& sm, const float basis[9],
                                             const ShT* __restrict__ sh, int lane) {
   constexpr int C = 3 * BD;
@@ -747,7 +755,7 @@ __device__ __forceinline__ void run_colours(int nR, bool have_prev, const WarpSm
     for (int j = 0; j < 8; ++j) {
       if ((need >> j) & 1u) {
         sm.rowlink[o] = lk[j];
-        sm.rowdst[o] = r * 8 + j;
+        sm.rowdst[o] = (short)(r * 8 + j);
         ++o;
       }
     }
@@ -789,7 +797,7 @@ __device__ __forceinline__ void run_colours(int nR, bool have_prev, const WarpSm
     __syncwarp();
     if (lane < nrow) {
       const int dst = sm.rowdst[m0 + lane];
-      float* out = sm.slot + (dst >> 3) * kSlotStride + (dst & 7) * 3;
+      float* out = sm.slot + (dst >> 3) * SS + (dst & 7) * 3;
       if constexpr (std::is_same<ShT, float>::value) {
         const float* row = sm.tile + lane * C;
 #pragma unroll
@@ -827,11 +835,11 @@ __device__ __forceinline__ void run_colours(int nR, bool have_prev, const WarpSm
     const int nd1 = two ? sm.run_need[q + 1] : 0xFF, dl1 = two ? sm.run_delta[q + 1] : 0;
     if (cg < 3) {
       if (!((nd0 >> cj) & 1))
-        sm.slot[q * kSlotStride + cj * 3 + cg] = sm.slot[(q - 1) * kSlotStride + (cj + dl0) * 3 + cg];
+        sm.slot[q * SS + cj * 3 + cg] = sm.slot[(q - 1) * SS + (cj + dl0) * 3 + cg];
       if (!((nd1 >> cj) & 1)) {
         const int j = cj + dl1;   // the corner's index in run q
-        const int src = ((nd0 >> j) & 1) ? q * kSlotStride + j * 3 : (q - 1) * kSlotStride + (j + dl0) * 3;
-        sm.slot[(q + 1) * kSlotStride + cj * 3 + cg] = sm.slot[src + cg];
+        const int src = ((nd0 >> j) & 1) ? q * SS + j * 3 : (q - 1) * SS + (j + dl0) * 3;
+        sm.slot[(q + 1) * SS + cj * 3 + cg] = sm.slot[src + cg];
       }
     }
     __syncwarp();
@@ -839,8 +847,9 @@ __device__ __forceinline__ void run_colours(int nR, bool have_prev, const WarpSm
 }
 
 // Colour (before the +0.5 offset) of the lane's sample from its run's corners.
+template <int SS>
 __device__ __forceinline__ void lane_colour(const WarpSmem& sm, int slot, const float w[8], float col[3]) {
-  const float* d = sm.slot + slot * kSlotStride;
+  const float* d = sm.slot + slot * SS;
   float c0 = 0.f, c1 = 0.f, c2 = 0.f;
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
@@ -1381,11 +1390,13 @@ __device__ __forceinline__ void bg_backward(const BgArgs& b, float lt, float g0,
 
 // The adjoint modes that keep segment checkpoints in shared memory (the two-kernel step needs
 // none: its reverse kernel reads every evaluated sample from the record), and the blocks per SM
-// each mode is compiled for.  The reverse kernel of the
-// two-kernel step fits six (80 registers, 48 bytes spilled: 2% faster than five at 96).
+// each mode is compiled for: six (80 registers) for the forward kernels and the two-kernel
+// step's reverse, four (128 registers) for the one-kernel adjoint.  The forward kernels with the
+// MSI background or of the batch launch keep five (96 registers): at 80 they spill, and the
+// background's forward was 3% slower at six.
 __host__ __device__ constexpr bool ck_in_smem(int mode) { return mode == kFused || mode == kBwd; }
-__host__ __device__ constexpr int blocks_per_sm_bound(int mode) {
-  return mode == kFusedRev ? 6 : (mode == kFwd || mode == kFusedFwd) ? 5 : kAdjointBlocksPerSm;
+__host__ __device__ constexpr int blocks_per_sm_bound(int mode, bool multi, bool bg) {
+  return mode == kFusedRev ? 6 : (mode == kFwd || mode == kFusedFwd) ? (multi || bg ? 5 : 6) : kAdjointBlocksPerSm;
 }
 
 template <int BD, typename ShT, int MODE, bool IMAGE, bool MULTI, bool BG = false>
@@ -1394,7 +1405,8 @@ template <int BD, typename ShT, int MODE, bool IMAGE, bool MULTI, bool BG = fals
 // more than the registers a larger budget would save.  The forward-only kernel and the two
 // kernels of the two-kernel fused step (no colour cache in shared memory; the forward keeps no
 // checkpoints there, the reverse gathers no rows) fit five blocks at 102 registers.
-__global__ void __launch_bounds__(kThreads, blocks_per_sm_bound(MODE)) render_kernel(GridP g0, OptP opt, IoP io) {
+__global__ void __launch_bounds__(kThreads, blocks_per_sm_bound(MODE, MULTI, BG)) render_kernel(GridP g0, OptP opt,
+                                                                                         IoP io) {
   constexpr int C = 3 * BD;
   constexpr bool kSplit = MODE == kFusedFwd || MODE == kFusedRev;
   extern __shared__ float4 smem4[];
@@ -1406,8 +1418,10 @@ __global__ void __launch_bounds__(kThreads, blocks_per_sm_bound(MODE)) render_ke
   // Samples past the capacity are gathered again.
   const int scap = (io.gcol != nullptr || kSplit) ? 0 : io.cap;  // samples in the shared-memory cache
   constexpr int TR = tile_rows<ShT, MODE>();
-  float* wbase = reinterpret_cast<float*>(smem4) + (size_t)wib * warp_smem_floats(C, scap, ck_in_smem(MODE), TR);
-  const WarpSmem sm = carve(wbase, C, scap, ck_in_smem(MODE), TR);
+  constexpr int SS = slot_stride(MODE);
+  float* wbase = reinterpret_cast<float*>(smem4) +
+                 (size_t)wib * warp_smem_floats(C, scap, ck_in_smem(MODE), TR, SS, has_walk(MODE));
+  const WarpSmem sm = carve(wbase, C, scap, ck_in_smem(MODE), TR, SS, has_walk(MODE));
   const long long gslot = (long long)blockIdx.x * kWarps + wib;
   const bool gown = io.gcol != nullptr && gslot < io.gcol_warps;
   // one float4 per evaluated sample: its colour (before the +0.5 offset) and the log
@@ -1552,12 +1566,12 @@ __global__ void __launch_bounds__(kThreads, blocks_per_sm_bound(MODE)) render_ke
         }
         int slot;
         const int nR = segment_runs(s, have_prev, prev_base, sm, lane, &slot);
-        run_colours<BD, ShT, TR>(nR, have_prev, sm, basis, sh, lane);
+        run_colours<BD, ShT, TR, SS>(nR, have_prev, sm, basis, sh, lane);
         const bool ev = (s.evm >> lane) & 1u;
         if (ev) {
           float w8[8], col[3];
           corner_weights(s.pos[0], s.pos[1], s.pos[2], w8);
-          lane_colour(sm, slot, w8, col);
+          lane_colour<SS>(sm, slot, w8, col);
           const float w = sample_weight(s.lt_before, s.pcnt);
           acc0 = fmaf(w, fmaxf(__fadd_rn(col[0], 0.5f), 0.f), acc0);
           acc1 = fmaf(w, fmaxf(__fadd_rn(col[1], 0.5f), 0.f), acc1);
@@ -1575,7 +1589,7 @@ __global__ void __launch_bounds__(kThreads, blocks_per_sm_bound(MODE)) render_ke
         prev_base = __shfl_sync(kFull, s.base, last);
         __syncwarp();
         if (nR > 0) {
-          if (lane < 24) sm.slot[(lane >> 3) + 3 * (lane & 7)] = sm.slot[nR * kSlotStride + (lane >> 3) + 3 * (lane & 7)];
+          if (lane < 24) sm.slot[(lane >> 3) + 3 * (lane & 7)] = sm.slot[nR * SS + (lane >> 3) + 3 * (lane & 7)];
           if (lane < 3) sm.run_l[lane] = sm.run_l[nR * 3 + lane];
         }
         have_prev = true;
@@ -1691,8 +1705,8 @@ __global__ void __launch_bounds__(kThreads, blocks_per_sm_bound(MODE)) render_ke
         } else {
           // colours past the cache: gather again (the two-kernel step's records hold them all)
           if constexpr (TR > 0) {
-            run_colours<BD, ShT, TR>(nR, false, sm, basis, sh, lane);
-            if (ev) lane_colour(sm, slot, w8, col);
+            run_colours<BD, ShT, TR, SS>(nR, false, sm, basis, sh, lane);
+            if (ev) lane_colour<SS>(sm, slot, w8, col);
           }
         }
         // d(loss)/d(colour) pieces, trace_ray_cuvol_backward cuvol.cu:311-344
@@ -1724,10 +1738,10 @@ __global__ void __launch_bounds__(kThreads, blocks_per_sm_bound(MODE)) render_ke
         const float a2 = sc2 >= 0.f ? __fmul_rn(w, gout2) : 0.f;
         // accumulate per run: slot[r][g*8 + j] (g = 3: density)
         __syncwarp();  // colours read from the slots (re-gather path) are consumed
-        for (int q = lane; q < (nR + 1) * kSlotStride; q += 32) sm.slot[q] = 0.f;
+        for (int q = lane; q < (nR + 1) * SS; q += 32) sm.slot[q] = 0.f;
         __syncwarp();
         if (ev) {
-          float* d = sm.slot + slot * kSlotStride;
+          float* d = sm.slot + slot * SS;
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
             atomicAdd(d + 0 * 8 + j, __fmul_rn(w8[j], a0));
@@ -1764,7 +1778,7 @@ __global__ void __launch_bounds__(kThreads, blocks_per_sm_bound(MODE)) render_ke
             B = fresh ? 0.f : moved;
             lk_lane = sm.links[sm.run_lane[q] * 8 + cj];
           }
-          B = __fadd_rn(B, sm.slot[q * kSlotStride + lane]);
+          B = __fadd_rn(B, sm.slot[q * SS + lane]);
         }
         if (nR > 0) {
           bcell[0] = sm.run_l[3];
@@ -1863,7 +1877,8 @@ int launch_t(const GridP& g, const OptP& opt, IoP io, long long n_rays, cudaStre
   if (MODE == kFwd) io.gcol = nullptr;
   const size_t smem = sizeof(float) *
                       (size_t)warp_smem_floats(C, (io.gcol != nullptr || MODE == kFusedFwd || MODE == kFusedRev) ? 0 : cap,
-                                               ck_in_smem(MODE), tile_rows<ShT, MODE>()) *
+                                               ck_in_smem(MODE), tile_rows<ShT, MODE>(), slot_stride(MODE),
+                                               has_walk(MODE)) *
                       kWarps;
   // The function's dynamic shared-memory limit is one attribute per device for every
   // configuration (colour cache in shared or global memory, its capacity), so it is only ever

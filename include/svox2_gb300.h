@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define SVX_ABI_VERSION 2
+#define SVX_ABI_VERSION 3
 
 /* Status codes.  The reference raised RuntimeError through TORCH_CHECK
  * (svox2/csrc/include/data_spec.hpp:32-51); the ABI returns these instead and
@@ -262,12 +262,15 @@ typedef struct {
  *               at each ray's own index.
  *   work        device uint64 scratch of the caller (cleared by the call)
  *   colour_cache  NULL, or device memory of colour_cache_bytes (16-byte
- *               aligned) in which the fused mode keeps each ray's per-sample
- *               colours for its reverse pass; svx_batch_colour_cache_bytes(n)
- *               sizes it for rays of up to n evaluated samples.  Without it
- *               (or when it is too small for 32 samples a ray) the cache is
- *               48 samples in shared memory, and longer rays gather their
- *               colours again.
+ *               aligned) for the fused mode.  At least
+ *               svx_batch_record_bytes(max_rays, n) bytes (n >= 64), without
+ *               the MSI background: the step runs as two kernels with a record
+ *               of n samples per ray there, and rays with more evaluated
+ *               samples are redone by the one-kernel step.  Otherwise, at least
+ *               svx_batch_colour_cache_bytes(n) bytes (n >= 32): the one-kernel
+ *               step keeps each ray's per-sample colours there for its reverse
+ *               pass.  Without it the cache is 48 samples in shared memory, and
+ *               longer rays gather their colours again.
  * Allocates nothing.  max_rays sizes the persistent grid. */
 int svx_render_batch(int32_t mode, const svx_batch_grid_t* grids, int32_t basis_dim, int32_t sh_dtype,
                      int32_t with_background, const float* origins, const float* dirs, const int32_t* ray_grid,
@@ -279,6 +282,12 @@ int svx_render_batch(int32_t mode, const svx_batch_grid_t* grids, int32_t basis_
  * evaluated samples for every warp the batch launch keeps resident on the
  * current device (16 bytes a sample). */
 int64_t svx_batch_colour_cache_bytes(int32_t samples_per_ray);
+
+/* Bytes of a svx_render_batch colour cache that holds, for each of max_rays
+ * rays, a record of samples_per_ray evaluated samples (rounded up to 32; 24
+ * bytes a sample and a 32-byte header), after a 16-byte counter and an int32
+ * list of max_rays entries.  No counterpart in the reference. */
+int64_t svx_batch_record_bytes(int64_t max_rays, int32_t samples_per_ray);
 
 /* Coherence order of a ray table against one grid: order_out[i] = index_base +
  * the index of the i-th ray sorted by (octahedral direction bucket, Morton code

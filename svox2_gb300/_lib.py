@@ -14,7 +14,7 @@ from pathlib import Path
 
 from . import _build
 
-ABI_VERSION = 2
+ABI_VERSION = 3
 
 SVX_OK = 0
 SVX_ERR_INVALID = 1
@@ -113,6 +113,7 @@ SIGNATURES = {
     "svx_render_batch": [_i32, _vp, _i32, _i32, _i32, _vp, _vp, _vp, _vp, _vp, _i64, P(SvxRenderOpts), _vp, _vp,
                          _vp, _vp, _i64, _vp],
     "svx_batch_colour_cache_bytes": [_i32],
+    "svx_batch_record_bytes": [_i64, _i32],
     "svx_ray_order": [P(SvxGrid), P(SvxRays), P(SvxRenderOpts), _i32, _vp, _vp],
     "svx_add_accum": [_vp, _i32, _i32, _i64, _vp, _vp, _vp],
     "svx_camera_rays": [P(SvxCamera), _vp, _vp, _vp],
@@ -163,7 +164,8 @@ def load() -> C.CDLL:
             fn = getattr(lib, name)
             fn.argtypes = argtypes
             fn.restype = (C.c_char_p if name == "svx_last_error" else
-                          C.c_int64 if name == "svx_batch_colour_cache_bytes" else C.c_int)
+                          C.c_int64 if name in ("svx_batch_colour_cache_bytes", "svx_batch_record_bytes")
+                          else C.c_int)
         v = lib.svx_abi_version()
         if v != ABI_VERSION:
             raise ImportError(f"libsvox2_gb300 ABI version {v}, expected {ABI_VERSION}; rebuild the library")

@@ -833,6 +833,22 @@ extern "C" int svx_camera_rays(const svx_camera_t* cam, float* origins, float* d
   return SVX_OK;
 }
 
+// The batch launch's kernels (SH9, multi-grid) by SH storage type.
+template <int MODE>
+static int launch_batch(int dt, const GridP& g, const OptP& o, const IoP& io, long long n, cudaStream_t st) {
+  switch (dt) {
+    case SVX_F32: return launch_t<9, float, MODE, false, true>(g, o, io, n, st);
+    case SVX_BF16: return launch_t<9, __nv_bfloat16, MODE, false, true>(g, o, io, n, st);
+    case SVX_F16: return launch_t<9, __half, MODE, false, true>(g, o, io, n, st);
+  }
+  set_error("sh_dtype %d unknown", dt);
+  return SVX_ERR_INVALID;
+}
+
+// Bytes before the records in a batch launch's record buffer: the overflow counter (16 bytes) and
+// the overflow list (an int32 per ray), rounded up to 16.
+static long long batch_record_head(long long max_rays) { return 16 + ((4 * max_rays + 15) & ~15ll); }
+
 extern "C" int svx_render_batch(int32_t mode, const svx_batch_grid_t* grids, int32_t basis_dim, int32_t sh_dtype,
                                 int32_t with_background, const float* origins, const float* dirs, const int32_t* ray_grid,
                                 const int32_t* order, const int64_t* n_rays_dev, int64_t max_rays,
@@ -861,9 +877,42 @@ extern "C" int svx_render_batch(int32_t mode, const svx_batch_grid_t* grids, int
   io.n_rays_dev = reinterpret_cast<const long long*>(n_rays_dev);
   io.work = reinterpret_cast<unsigned long long*>(work);
   io.cap = g_cap;
+  GridP g{};  // per-ray grids come from the descriptors
+  cudaStream_t st = as_stream(stream);
   if (mode == 1 && colour_cache != nullptr) {
     SVX_REQUIRE((reinterpret_cast<uintptr_t>(colour_cache) & 15u) == 0, SVX_ERR_INVALID,
                 "colour_cache must be 16-byte aligned");
+  }
+  if (mode == 1 && colour_cache != nullptr && !with_background) {
+    // the two-kernel step when the buffer holds a record of at least 64 samples for each of
+    // max_rays rays (svx_batch_record_bytes): the overflow counter and list, then the records
+    const long long head = batch_record_head(max_rays);
+    const long long per = colour_cache_bytes > head ? (colour_cache_bytes - head) / max_rays / 16 : 0;
+    const long long cap = std::min<long long>(per > 2 ? ((per - 2) * 2 / 3) & ~31ll : 0, kGlobalCapMax);
+    if (cap >= 64) {
+      char* base = reinterpret_cast<char*>(colour_cache);
+      io.ovf_count = reinterpret_cast<unsigned long long*>(base);
+      io.ovf_list = reinterpret_cast<int*>(base + 16);
+      io.rec = reinterpret_cast<float4*>(base + head);
+      io.rec_stride = 2 + cap + cap / 2;
+      io.cap = (int)cap;
+      SVX_CUDA_TRY(cudaMemsetAsync(io.ovf_count, 0, sizeof(unsigned long long), st));
+      int rc2 = launch_batch<kFusedFwd>(sh_dtype, g, o, io, max_rays, st);
+      if (rc2) return rc2;
+      rc2 = launch_batch<kFusedRev>(sh_dtype, g, o, io, max_rays, st);
+      if (rc2) return rc2;
+      // the rays whose samples did not fit their record, in the one-kernel step
+      IoP iov = io;
+      iov.order = io.ovf_list;
+      iov.n_rays_dev = reinterpret_cast<const long long*>(io.ovf_count);
+      iov.rec = nullptr;
+      iov.ovf_count = nullptr;
+      iov.ovf_list = nullptr;
+      iov.cap = g_cap;
+      return launch_batch<kFused>(sh_dtype, g, o, iov, max_rays, st);
+    }
+  }
+  if (mode == 1 && colour_cache != nullptr) {
     const long long warps = (long long)num_sms() * kAdjointBlocksPerSm * kWarps;
     const long long cap = colour_cache_bytes / (long long)sizeof(float4) / warps;
     if (cap >= 32) {
@@ -872,22 +921,15 @@ extern "C" int svx_render_batch(int32_t mode, const svx_batch_grid_t* grids, int
       io.cap = (int)std::min<long long>(cap, kGlobalCapMax);
     }
   }
-  GridP g{};  // per-ray grids come from the descriptors
-  cudaStream_t st = as_stream(stream);
   if (with_background) return dispatch_bg_batch(mode == 0 ? kFwd : kFused, sh_dtype, g, o, io, max_rays, st);
-  switch (sh_dtype) {
-    case SVX_F32:
-      return mode == 0 ? launch_t<9, float, kFwd, false, true>(g, o, io, max_rays, st)
-                       : launch_t<9, float, kFused, false, true>(g, o, io, max_rays, st);
-    case SVX_BF16:
-      return mode == 0 ? launch_t<9, __nv_bfloat16, kFwd, false, true>(g, o, io, max_rays, st)
-                       : launch_t<9, __nv_bfloat16, kFused, false, true>(g, o, io, max_rays, st);
-    case SVX_F16:
-      return mode == 0 ? launch_t<9, __half, kFwd, false, true>(g, o, io, max_rays, st)
-                       : launch_t<9, __half, kFused, false, true>(g, o, io, max_rays, st);
-  }
-  set_error("sh_dtype %d unknown", sh_dtype);
-  return SVX_ERR_INVALID;
+  return mode == 0 ? launch_batch<kFwd>(sh_dtype, g, o, io, max_rays, st)
+                   : launch_batch<kFused>(sh_dtype, g, o, io, max_rays, st);
+}
+
+extern "C" int64_t svx_batch_record_bytes(int64_t max_rays, int32_t samples_per_ray) {
+  if (max_rays <= 0 || samples_per_ray <= 0) return 0;
+  const long long cap = std::min<long long>(((long long)samples_per_ray + 31) & ~31ll, kGlobalCapMax);
+  return batch_record_head(max_rays) + max_rays * (2 + cap + cap / 2) * 16;
 }
 
 extern "C" int64_t svx_batch_colour_cache_bytes(int32_t samples_per_ray) {

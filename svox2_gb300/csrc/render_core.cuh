@@ -123,6 +123,10 @@ struct IoP {
   int gcol_bg;     // background shells each slice also holds (4 float4 each, after the cap entries)
   float4* rec;     // kFusedFwd / kFusedRev: one record of rec_stride entries per ray position
   long long rec_stride;  // 2 + cap + cap / 2 (header, colour entries, (t, sigma) pairs)
+  // kFusedFwd of a batch launch: rays with more evaluated samples than a record holds are listed
+  // here (ray indices) for the one-kernel step; null where cap bounds every ray
+  unsigned long long* ovf_count;
+  int* ovf_list;
   // MSI background (grids that have one; render_kernel<..., BG = true>)
   const int32_t* bg_links;     // [2 reso, reso]
   const float* bg_data;        // [bg_cap, bg_nl, 4], rows 16-byte aligned
@@ -1391,12 +1395,12 @@ __device__ __forceinline__ void bg_backward(const BgArgs& b, float lt, float g0,
 // The adjoint modes that keep segment checkpoints in shared memory (the two-kernel step needs
 // none: its reverse kernel reads every evaluated sample from the record), and the blocks per SM
 // each mode is compiled for: six (80 registers) for the forward kernels and the two-kernel
-// step's reverse, four (128 registers) for the one-kernel adjoint.  The forward kernels with the
-// MSI background or of the batch launch keep five (96 registers): at 80 they spill, and the
-// background's forward was 3% slower at six.
+// step's reverse, four (128 registers) for the one-kernel adjoint.  Those with the MSI background
+// or of the batch launch keep five (96 registers): at 80 they spill, and the background's
+// forward was 3% slower at six.
 __host__ __device__ constexpr bool ck_in_smem(int mode) { return mode == kFused || mode == kBwd; }
 __host__ __device__ constexpr int blocks_per_sm_bound(int mode, bool multi, bool bg) {
-  return mode == kFusedRev ? 6 : (mode == kFwd || mode == kFusedFwd) ? (multi || bg ? 5 : 6) : kAdjointBlocksPerSm;
+  return (mode == kFwd || mode == kFusedFwd || mode == kFusedRev) ? (multi || bg ? 5 : 6) : kAdjointBlocksPerSm;
 }
 
 template <int BD, typename ShT, int MODE, bool IMAGE, bool MULTI, bool BG = false>
@@ -1469,7 +1473,7 @@ __global__ void __launch_bounds__(kThreads, blocks_per_sm_bound(MODE, MULTI, BG)
       tsig_out = reinterpret_cast<float2*>(rec + 2 + cap);
     }
     if constexpr (MODE == kFusedRev) {
-      if (__float_as_int(rec[1].x) == 0) {   // no evaluated sample: no gradient
+      if (__float_as_int(rec[1].x) <= 0) {   // no evaluated sample, or a ray left to the one-kernel step
         next = __shfl_sync(kFull, next, 0);
         continue;
       }
@@ -1674,7 +1678,13 @@ __global__ void __launch_bounds__(kThreads, blocks_per_sm_bound(MODE, MULTI, BG)
       if constexpr (MODE == kFusedFwd) {
         if (lane == 0) {   // the record's header
           rec[0] = make_float4(gout0, gout1, gout2, carry);
-          rec[1] = make_float4(__int_as_float(n_eval), 0.f, 0.f, 0.f);
+          if (n_eval > cap && io.ovf_list != nullptr) {
+            // the record could not hold every sample: the one-kernel step redoes this ray
+            rec[1] = make_float4(__int_as_float(-1), 0.f, 0.f, 0.f);
+            io.ovf_list[atomicAdd(io.ovf_count, 1ull)] = (int)ray;
+          } else {
+            rec[1] = make_float4(__int_as_float(n_eval), 0.f, 0.f, 0.f);
+          }
         }
       }
     }

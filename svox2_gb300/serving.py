@@ -310,9 +310,10 @@ class RenderServer:
                 "desc_version": -1,      # version of desc_host last uploaded to this lane
                 "graph": None,
             }
-        # the train lane's colour cache: per-sample colours of rays up to 1024 evaluated samples
-        # (the longest ray of a 256^3 grid at step 0.5 has 887 samples)
-        cache_bytes = int(_lib.load().svx_batch_colour_cache_bytes(1024))
+        # the train lane's records for the two-kernel fused step: each ray's per-sample colour,
+        # transmittance, t and sigma, up to 1024 evaluated samples (the longest ray of a 256^3
+        # grid at step 0.5 has 887; longer rays are redone by the one-kernel step)
+        cache_bytes = int(_lib.load().svx_batch_record_bytes(B, 1024))
         self.lanes["train"]["colour_cache"] = torch.empty((cache_bytes // 4,), dtype=torch.float32, device=dev)
         lane_bytes = sum(t.numel() * t.element_size() for lane in self.lanes.values() for t in lane.values()
                          if isinstance(t, torch.Tensor))

@@ -40,7 +40,8 @@ def _order(spec, o, d, opt, base, out):
               base, out.data_ptr(), torch.cuda.current_stream().cuda_stream)
 
 
-def _batch(mode, grids, rays, opt, sh_dtype, use_order, accum_for=(), with_bg=0, cache_samples=0):
+def _batch(mode, grids, rays, opt, sh_dtype, use_order, accum_for=(), with_bg=0, cache_samples=0,
+           record_samples=0):
     """One svx_render_batch launch over every grid's rays; returns rgb per grid and the
     per-grid gradient buffers (accumulation rows already flushed)."""
     dev = "cuda"
@@ -86,6 +87,9 @@ def _batch(mode, grids, rays, opt, sh_dtype, use_order, accum_for=(), with_bg=0,
     if cache_samples:
         nbytes = int(_lib.load().svx_batch_colour_cache_bytes(cache_samples))
         cache = torch.empty((nbytes // 4,), dtype=torch.float32, device=dev)
+    if record_samples:
+        nbytes = int(_lib.load().svx_batch_record_bytes(n, record_samples))
+        cache = torch.empty((nbytes // 4,), dtype=torch.float32, device=dev)
     _lib.call("svx_render_batch", mode, table.data_ptr(), 9, dt, with_bg, O_.data_ptr(), D_.data_ptr(),
               ray_grid.data_ptr(),
               order.data_ptr() if use_order else None, n_dev.data_ptr(), n, C.byref(csrc._opt_struct(opt)),
@@ -105,15 +109,20 @@ def _batch(mode, grids, rays, opt, sh_dtype, use_order, accum_for=(), with_bg=0,
     return out, bufs
 
 
-@pytest.mark.parametrize("cache_samples", [0, 64], ids=["smem_cache", "global_cache"])
+@pytest.mark.parametrize("cache", [(0, 0), (64, 0), (0, 64), (0, 512)],
+                         ids=["smem_cache", "global_cache", "records_overflow", "records"])
 @pytest.mark.parametrize("sh_dtype", [torch.float32, torch.bfloat16])
 @pytest.mark.parametrize("use_order", [False, True])
-def test_batch_fused_matches_oracle_per_grid(sh_dtype, use_order, cache_samples):
+def test_batch_fused_matches_oracle_per_grid(sh_dtype, use_order, cache):
     """Without a colour cache buffer the fused batch keeps 48 samples a ray in shared memory;
-    with one of 64 samples a ray, rays longer than that gather colours again past it."""
+    with one of 64 samples a ray, rays longer than that gather colours again past it.  With a
+    record buffer it runs as two kernels: with records of 64 samples the rays that evaluate more
+    are listed and redone by the one-kernel step; with 512 every ray fits."""
+    cache_samples, record_samples = cache
     opt, oopt = opt_struct()
     grids, rays = _setup(sh_dtype)
-    rgbs, bufs = _batch(1, grids, rays, opt, sh_dtype, use_order, accum_for=(1,), cache_samples=cache_samples)
+    rgbs, bufs = _batch(1, grids, rays, opt, sh_dtype, use_order, accum_for=(1,), cache_samples=cache_samples,
+                        record_samples=record_samples)
     for (spec, og), (o, d, gt), rgb, b in zip(grids, rays, rgbs, bufs):
         ref = O.render(og, oopt, o.numpy(), d.numpy(), mode=1, rgb_gt=gt.numpy(), prec="f32")
         r64 = O.render(og, oopt, o.numpy(), d.numpy(), mode=1, rgb_gt=gt.numpy(), prec="f64", stops=ref["stops"],

@@ -628,7 +628,7 @@ def run_serve(args):
     total_rays = sum(r.width * r.height if isinstance(r, RenderRequest) else r.origins.shape[0] for r in reqs)
 
     # ---- continuous batching
-    server = RenderServer(device=dev, hbm_budget=150e9, batch_rays=1 << 20, chunk_rays=1 << 18)
+    server = RenderServer(device=dev, hbm_budget=150e9, batch_rays=1 << 20, chunk_rays=args.chunk_rays)
     for k, g in datas.items():
         server.add_grid(k, fresh(g), trainable=True)
     # warm-up: one request of each kind (graphs captured, kernels loaded), not timed
@@ -678,11 +678,17 @@ def run_serve(args):
     lat = np.array(lat)
     stats_s = {"n": int(lat.size), "p50_ms": float(np.percentile(lat, 50) * 1e3),
                "p99_ms": float(np.percentile(lat, 99) * 1e3), "mean_ms": float(lat.mean() * 1e3)}
+    for kind, cls in (("render", RenderRequest), ("train", TrainRequest)):
+        lk = np.array([x for x, r in zip(lat, reqs) if isinstance(r, cls)])
+        if lk.size:
+            stats_s[f"{kind}_p50_ms"] = float(np.percentile(lk, 50) * 1e3)
+            stats_s[f"{kind}_p99_ms"] = float(np.percentile(lk, 99) * 1e3)
     line = {"metric": "serving: requests/s and p50/p99 latency, continuous batching vs serial plain launches",
             "unit": "requests/s", "value": n_req / span_b, "data": "synthetic",
             "config": {"workload": "Poisson %.0f req/s, %d requests, 50%% renders (side U{64..800}) / 50%% train "
                                    "steps (logU[4096, 262144] rays), 16 grids 128^3..256^3 5-25%% occupancy BF16 SH, "
-                                   "150 GB budget" % (args.rate, n_req), "total_rays": int(total_rays)},
+                                   "150 GB budget" % (args.rate, n_req), "total_rays": int(total_rays),
+                       "batch_rays": 1 << 20, "chunk_rays": args.chunk_rays},
             "batched": {"requests_per_s": n_req / span_b, "rays_per_s": total_rays / span_b, "makespan_s": span_b,
                         **stats_b, "batches": server.batches},
             "serial": {"requests_per_s": n_req / span_s, "rays_per_s": total_rays / span_s, "makespan_s": span_s,
@@ -809,6 +815,7 @@ def main():
     ap.add_argument("--bg-reso", type=int, default=1024, help="background: MSI resolution (T&T: 1024)")
     ap.add_argument("--rate", type=float, default=2000.0, help="serve: Poisson arrival rate (requests/s)")
     ap.add_argument("--rates", default="", help="serve: comma-separated arrival rates, one line each (overrides --rate)")
+    ap.add_argument("--chunk-rays", type=int, default=1 << 18, help="serve: rays of a render request per batch")
     args = ap.parse_args()
     if args.config == "mixed":
         run_mixed(args)

@@ -656,9 +656,16 @@ class RenderServer:
 
 
 def latency_stats(tickets: List[Ticket]) -> dict:
+    """Latency percentiles of the finished tickets, over all and per kind (render / train)."""
     lat = np.array([t.latency for t in tickets if t.state == "done"], dtype=np.float64)
     if lat.size == 0:
         return {"n": 0}
-    return {"n": int(lat.size), "p50_ms": float(np.percentile(lat, 50) * 1e3),
-            "p99_ms": float(np.percentile(lat, 99) * 1e3), "mean_ms": float(lat.mean() * 1e3),
-            "max_ms": float(lat.max() * 1e3)}
+    out = {"n": int(lat.size), "p50_ms": float(np.percentile(lat, 50) * 1e3),
+           "p99_ms": float(np.percentile(lat, 99) * 1e3), "mean_ms": float(lat.mean() * 1e3),
+           "max_ms": float(lat.max() * 1e3)}
+    for kind in ("render", "train"):
+        lk = np.array([t.latency for t in tickets if t.state == "done" and t.kind == kind], dtype=np.float64)
+        if lk.size:
+            out[f"{kind}_p50_ms"] = float(np.percentile(lk, 50) * 1e3)
+            out[f"{kind}_p99_ms"] = float(np.percentile(lk, 99) * 1e3)
+    return out

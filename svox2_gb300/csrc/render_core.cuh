@@ -1394,13 +1394,14 @@ __device__ __forceinline__ void bg_backward(const BgArgs& b, float lt, float g0,
 
 // The adjoint modes that keep segment checkpoints in shared memory (the two-kernel step needs
 // none: its reverse kernel reads every evaluated sample from the record), and the blocks per SM
-// each mode is compiled for: six (80 registers) for the forward kernels and the two-kernel
-// step's reverse, four (128 registers) for the one-kernel adjoint.  Those with the MSI background
-// or of the batch launch keep five (96 registers): at 80 they spill, and the background's
-// forward was 3% slower at six.
+// each mode is compiled for: six (80 registers) for the forward kernels, seven (72 registers,
+// 76 bytes spilled, 2.3% faster than six) for the two-kernel step's reverse, four (128
+// registers) for the one-kernel adjoint.  Those with the MSI background or of the batch launch
+// keep five (96 registers): at 80 they spill, and the background's forward was 3% slower at six.
 __host__ __device__ constexpr bool ck_in_smem(int mode) { return mode == kFused || mode == kBwd; }
 __host__ __device__ constexpr int blocks_per_sm_bound(int mode, bool multi, bool bg) {
-  return (mode == kFwd || mode == kFusedFwd || mode == kFusedRev) ? (multi || bg ? 5 : 6) : kAdjointBlocksPerSm;
+  if (mode == kFwd || mode == kFusedFwd || mode == kFusedRev) return multi || bg ? 5 : mode == kFusedRev ? 7 : 6;
+  return kAdjointBlocksPerSm;
 }
 
 template <int BD, typename ShT, int MODE, bool IMAGE, bool MULTI, bool BG = false>

@@ -621,10 +621,11 @@ class RenderServer:
                     grid.sparse_background_indexer = None
                 grid.sparse_grad_indexer = None
                 grid.sparse_sh_grad_indexer = None
-            ev = torch.cuda.Event()
-            ev.record(st)
-        for t in trains:
-            t.rays_done_event.append(ev)
+                # the request is complete once its grid's step is: an event of its own, so that
+                # it does not wait for the optimiser steps of the batch's later grids
+                ev = torch.cuda.Event()
+                ev.record(st)
+                t.rays_done_event.append(ev)
         lane["queued"].append(ev)
 
     def _collect(self) -> List[Ticket]:

@@ -628,7 +628,8 @@ def run_serve(args):
     total_rays = sum(r.width * r.height if isinstance(r, RenderRequest) else r.origins.shape[0] for r in reqs)
 
     # ---- continuous batching
-    server = RenderServer(device=dev, hbm_budget=150e9, batch_rays=1 << 20, chunk_rays=args.chunk_rays)
+    server = RenderServer(device=dev, hbm_budget=150e9, batch_rays=args.batch_rays, chunk_rays=args.chunk_rays)
+    server.lane_depth = args.lane_depth
     for k, g in datas.items():
         server.add_grid(k, fresh(g), trainable=True)
     # warm-up: one request of each kind (graphs captured, kernels loaded), not timed
@@ -688,7 +689,7 @@ def run_serve(args):
             "config": {"workload": "Poisson %.0f req/s, %d requests, 50%% renders (side U{64..800}) / 50%% train "
                                    "steps (logU[4096, 262144] rays), 16 grids 128^3..256^3 5-25%% occupancy BF16 SH, "
                                    "150 GB budget" % (args.rate, n_req), "total_rays": int(total_rays),
-                       "batch_rays": 1 << 20, "chunk_rays": args.chunk_rays},
+                       "batch_rays": args.batch_rays, "chunk_rays": args.chunk_rays, "lane_depth": args.lane_depth},
             "batched": {"requests_per_s": n_req / span_b, "rays_per_s": total_rays / span_b, "makespan_s": span_b,
                         **stats_b, "batches": server.batches},
             "serial": {"requests_per_s": n_req / span_s, "rays_per_s": total_rays / span_s, "makespan_s": span_s,
@@ -816,6 +817,8 @@ def main():
     ap.add_argument("--rate", type=float, default=2000.0, help="serve: Poisson arrival rate (requests/s)")
     ap.add_argument("--rates", default="", help="serve: comma-separated arrival rates, one line each (overrides --rate)")
     ap.add_argument("--chunk-rays", type=int, default=1 << 18, help="serve: rays of a render request per batch")
+    ap.add_argument("--batch-rays", type=int, default=1 << 20, help="serve: rays per lane and iteration")
+    ap.add_argument("--lane-depth", type=int, default=2, help="serve: batches a lane may have queued")
     args = ap.parse_args()
     if args.config == "mixed":
         run_mixed(args)

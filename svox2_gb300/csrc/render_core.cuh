@@ -117,8 +117,9 @@ struct IoP {
   unsigned long long* work;    // ray counter (zeroed by the host)
   unsigned long long* eval_count;
   unsigned long long* trace;
-  int cap;         // colour cache capacity (samples per ray)
-  float* gcol;     // optional colour cache in global memory: one slice per resident warp
+  int cap;         // colour cache (or, two-kernel step, record) capacity: samples per ray
+  float* gcol;     // optional colour cache in global memory: one slice per resident warp (in the
+                   // two-kernel step's forward, the MSI background's shells only)
   long long gcol_warps;  // slices in gcol (warps of the launch)
   int gcol_bg;     // background shells each slice also holds (4 float4 each, after the cap entries)
   float4* rec;     // kFusedFwd / kFusedRev: one record of rec_stride entries per ray position

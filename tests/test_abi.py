@@ -154,3 +154,20 @@ def test_operator_module_has_the_reference_op_table():
         assert not hasattr(C, n)
     for cls in ("SparseGridSpec", "CameraSpec", "RaysSpec", "RenderOptions", "GridOutputGrads"):
         assert hasattr(C, cls)
+
+
+def test_batch_record_buffer_size():
+    """svx_batch_record_bytes (host arithmetic only): a 16-byte overflow counter, an int32
+    overflow list of max_rays entries rounded up to 16 bytes, then a record per ray of a 32-byte
+    header and 24 bytes for each of cap samples (samples_per_ray rounded up to 32, at most 4096)."""
+    from svox2_gb300 import _lib
+    lib = _lib.load()
+
+    def expect(n, spr):
+        cap = min((spr + 31) // 32 * 32, 4096)
+        return 16 + (4 * n + 15) // 16 * 16 + n * (2 + cap + cap // 2) * 16
+
+    for n, spr in ((1, 1), (3, 64), (1000, 1000), (1 << 20, 1024), (7, 5000)):
+        assert lib.svx_batch_record_bytes(n, spr) == expect(n, spr)
+    assert lib.svx_batch_record_bytes(0, 64) == 0
+    assert lib.svx_batch_record_bytes(10, 0) == 0

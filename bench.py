@@ -51,9 +51,9 @@ BYTES_PER_RAY = 48
 # DRAM bytes (read + write) per evaluated sample of the fused step on this workload (its two
 # kernels, render_kernel<9, float, kFusedFwd> and <9, float, kFusedRev>): one ncu capture of
 # three full 1M-ray steps (dram__bytes_read.sum and dram__bytes_write.sum only, a single replay
-# pass per launch) measured 25.13 GB (forward) + 31.97 GB (reverse) per step over 155.83 M
+# pass per launch) measured 25.19 GB (forward) + 38.50 GB (reverse) per step over 155.83 M
 # evaluated samples per step.
-DRAM_BYTES_PER_SAMPLE = 366.4
+DRAM_BYTES_PER_SAMPLE = 408.7
 # launches of this library per training step: ray_keys_kernel, 6 CUB radix-sort kernels,
 # render_kernel twice (the fused step's forward and reverse kernels), add_accum_kernel,
 # 2 x tv_sparse_kernel, 2 x step_mask_kernel

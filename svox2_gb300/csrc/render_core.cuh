@@ -298,42 +298,70 @@ constexpr int kSlotStride = 33;  // floats per slot (odd: lanes reading differen
 // Floats per slot by mode: the forward kernels keep 24 colour values a slot (8 corners x 3
 // groups), the adjoint 32 gradient sums (4 groups x 8 corners); both strides are odd, so lanes
 // reading different slots hit different banks.  The forward kernels also carve no run-walk
-// array: with these, their shared memory fits six blocks per SM.
+// array.
 __host__ __device__ constexpr int slot_stride(int mode) { return (mode == kFwd || mode == kFusedFwd) ? 25 : kSlotStride; }
 __host__ __device__ constexpr bool has_walk(int mode) { return !(mode == kFwd || mode == kFusedFwd); }
+// The adjoint modes that keep segment checkpoints in shared memory (the two-kernel step needs
+// none: its reverse kernel reads every evaluated sample from the record).
+__host__ __device__ constexpr bool ck_in_smem(int mode) { return mode == kFused || mode == kBwd; }
 
 // Coefficient rows gathered per pass.  Rows are copied into shared memory with cp.async, all rows
 // of a pass in flight at once (one memory round trip per pass, no registers held): 32 rows for
-// the adjoint instantiations, 24 for the forward ones, whose six blocks per SM leave less shared
-// memory per warp.  The reverse kernel of the two-kernel fused step gathers no rows (its
-// colours are in the records): 0, and no row tables.
+// the adjoint instantiations.  The forward ones take 12 FP32 rows (30 floats each) or 24 16-bit
+// rows (14 words each): their six blocks per SM then fit the 196 KB shared-memory carve-out and
+// leave 60 KB of the SM's 256 KB to L1, which holds the link and density gathers (FP32 forward
+// 7% faster than with 23 rows and 28 KB of L1).  The reverse kernel of the two-kernel fused step
+// gathers no rows (its colours are in the records): 0, and no row tables.
 template <typename ShT, int MODE>
 __host__ __device__ constexpr int tile_rows() {
-  return (MODE == kFwd || MODE == kFusedFwd) ? 24 : MODE == kFusedRev ? 0 : 32;
+  return (MODE == kFwd || MODE == kFusedFwd) ? (std::is_same<ShT, float>::value ? 12 : 24) : MODE == kFusedRev ? 0 : 32;
 }
 
 // 4-byte words a 16-bit row of C coefficients can span (it starts on a 2-byte boundary).
 __host__ __device__ constexpr int row_words16(int C) { return C / 2 + 1; }
 constexpr int kMaxRows = 8 * 32; // corner rows a segment can need
-constexpr int kFlushCap = 64;    // retiring corner rows listed before a flush pass
 
-__host__ __device__ constexpr int tile_floats(int C, int rows) {
-  return rows * C > kFlushCap * 5 ? rows * C : kFlushCap * 5;
+// Retiring corner rows the adjoint lists before a flush pass: 64, and 32 in the reverse kernel
+// of the two-kernel step, whose shared memory then fits eight blocks per SM (27 KB a block).
+// The forward kernels flush nothing.
+__host__ __device__ constexpr int flush_cap(int mode) {
+  return (mode == kFwd || mode == kFusedFwd) ? 0 : mode == kFusedRev ? 32 : 64;
+}
+
+// Floats between FP32 rows in the tile: C rounded up to an odd number of 8-byte words, so a lane
+// reads its row as float2 words and the 16 lanes of each half-warp hit distinct banks (30 floats
+// for SH9: 14 shared loads a row instead of 27).
+__host__ __device__ constexpr int row_stride32(int C) { return (((C + 1) >> 1) | 1) << 1; }
+
+// Floats a tile row takes for SH storage ShT.
+template <typename ShT>
+__host__ __device__ constexpr int tile_row_floats(int C) {
+  return std::is_same<ShT, float>::value ? row_stride32(C) : row_words16(C);
+}
+
+// rs: floats a tile row takes; fc: the flush list's rows (4 sums and a link each), which reuse the
+// tile.  A multiple of 4 floats: the corner links and optical depths carved after the tile are
+// moved as int4 / float4 words.
+__host__ __device__ constexpr int tile_floats(int rs, int rows, int fc) {
+  return ((rows * rs > fc * 5 ? rows * rs : fc * 5) + 3) & ~3;
 }
 
 struct WarpSmem {
   int* links;        // [32][8] corner links of the staged samples
   float* slot;       // [kSlots][slot stride]: D[j*3+g] (colour pass) or B[g*8+j] (adjoint)
-  float* tile;       // [rows][C] gathered coefficient rows; in the adjoint, the flush list
+  float* tile;       // [rows][row stride] gathered coefficient rows (16-byte aligned); in the
+                     // adjoint, the flush list
   int* rowlink;      // [kMaxRows] link of each row to gather
   short* rowdst;     // [kMaxRows] slot*8 + corner of each row
   int* run_lane;     // [kSlots] first lane of each run
   int* run_l;        // [kSlots][3] cell of each run
-  int* run_need;     // [kSlots] corners the run gathers (bit mask)
-  int* run_delta;    // [kSlots] index offset of a shared corner in the previous run
+  unsigned char* run_need;  // [kSlots] colour pass: corners the run gathers (bit mask)
+  signed char* run_delta;   // [kSlots] colour pass: index offset (-7..7) of a shared corner in the
+                            // previous run
   int* run_walk;     // [kSlots] adjoint: each run's transition from the run after it (walk_info)
                      // (none in the forward kernels)
-  float* pc;         // [32] forward-only march: the segment's optical depths (0 where not evaluated)
+  float* pc;         // [32] forward kernels' march: the segment's optical depths (0 where not
+                     // evaluated), right after links
   float* ck_t;       // [kNumCkpt]
   float* ck_lt;      // [kNumCkpt]
   int* ck_idx;       // [kNumCkpt]
@@ -344,34 +372,55 @@ struct WarpSmem {
   float* col;        // [cap][4] colour cache entries (16-byte aligned)
 };
 
-// adjoint: the reverse pass's checkpoint arrays are carved (the forward-only kernel has none,
-// which lets five of its blocks share an SM).  ss: floats per slot; walk: the run-walk array.
-__host__ __device__ constexpr int warp_smem_floats(int C, int cap, bool adjoint, int rows, int ss, bool walk) {
-  return (32 * 8 + 32 + kSlots * ss + tile_floats(C, rows) + (rows > 0 ? kMaxRows + kMaxRows / 2 : 0) +
-          kSlots * (walk ? 7 : 6) + (adjoint ? 3 * kNumCkpt + 3 * kMaxStride : 0) + 16 + 4 * cap + 3) & ~3;
+// What a warp's slice of shared memory holds in one instantiation; the host sizes the slice and
+// the kernel carves it from the same description.
+struct SmemLayout {
+  int rs;     // floats a tile row takes
+  int rows;   // tile rows (0: no row tables)
+  int fc;     // flush-list rows
+  int ss;     // floats per slot
+  int cap;    // colour-cache samples in shared memory
+  bool ckpt;  // the reverse pass's checkpoint arrays (the one-kernel adjoint)
+  bool walk;  // the run-walk array (adjoint)
+  bool plan;  // run_need / run_delta (colour pass)
+  bool pc;    // the optical depths of the forward kernels' march
+};
+
+template <typename ShT, int MODE>
+__host__ __device__ constexpr SmemLayout smem_layout(int C, int cap) {
+  return SmemLayout{tile_row_floats<ShT>(C), tile_rows<ShT, MODE>(), flush_cap(MODE), slot_stride(MODE), cap,
+                    ck_in_smem(MODE), has_walk(MODE), MODE != kFusedRev, MODE == kFwd || MODE == kFusedFwd};
 }
 
-__device__ __forceinline__ WarpSmem carve(float* base, int C, int cap, bool adjoint, int rows, int ss, bool walk) {
+__host__ __device__ constexpr int warp_smem_floats(const SmemLayout& L) {
+  return (tile_floats(L.rs, L.rows, L.fc) + 32 * 8 + (L.pc ? 32 : 0) + kSlots * L.ss +
+          (L.rows > 0 ? kMaxRows + kMaxRows / 2 : 0) + kSlots * (L.walk ? 5 : 4) + (L.plan ? (2 * kSlots + 3) / 4 : 0) +
+          (L.ckpt ? 3 * kNumCkpt + 3 * kMaxStride : 0) + 16 + 4 * L.cap + 3) & ~3;
+}
+
+__device__ __forceinline__ WarpSmem carve(float* base, const SmemLayout& L) {
   WarpSmem s;
-  const int nrow = rows > 0 ? kMaxRows : 0;
-  s.links = reinterpret_cast<int*>(base);
-  s.pc = base + 32 * 8;
-  s.slot = base + 32 * 8 + 32;
-  s.tile = s.slot + kSlots * ss;
-  s.rowlink = reinterpret_cast<int*>(s.tile + tile_floats(C, rows));
+  const int nrow = L.rows > 0 ? kMaxRows : 0;
+  // the tile first: the warp's base is 16-byte aligned (warp_smem_floats is a multiple of 4)
+  s.tile = base;
+  s.links = reinterpret_cast<int*>(base + tile_floats(L.rs, L.rows, L.fc));
+  s.pc = L.pc ? reinterpret_cast<float*>(s.links + 32 * 8) : nullptr;
+  s.slot = reinterpret_cast<float*>(s.links + 32 * 8) + (L.pc ? 32 : 0);
+  s.rowlink = reinterpret_cast<int*>(s.slot + kSlots * L.ss);
   s.rowdst = reinterpret_cast<short*>(s.rowlink + nrow);
   s.run_lane = s.rowlink + nrow + nrow / 2;
   s.run_l = s.run_lane + kSlots;
-  s.run_need = s.run_l + 3 * kSlots;
-  s.run_delta = s.run_need + kSlots;
-  s.run_walk = walk ? s.run_delta + kSlots : nullptr;
-  s.ck_t = reinterpret_cast<float*>(s.run_delta + kSlots + (walk ? kSlots : 0));
+  s.run_walk = L.walk ? s.run_l + 3 * kSlots : nullptr;
+  int* after = s.run_l + 3 * kSlots + (L.walk ? kSlots : 0);
+  s.run_need = L.plan ? reinterpret_cast<unsigned char*>(after) : nullptr;
+  s.run_delta = L.plan ? reinterpret_cast<signed char*>(after) + kSlots : nullptr;
+  s.ck_t = reinterpret_cast<float*>(after + (L.plan ? (2 * kSlots + 3) / 4 : 0));
   s.ck_lt = s.ck_t + kNumCkpt;
   s.ck_idx = reinterpret_cast<int*>(s.ck_lt + kNumCkpt);
   s.tmp_t = reinterpret_cast<float*>(s.ck_idx + kNumCkpt);
   s.tmp_lt = s.tmp_t + kMaxStride;
   s.tmp_idx = reinterpret_cast<int*>(s.tmp_lt + kMaxStride);
-  s.basis = adjoint ? reinterpret_cast<float*>(s.tmp_idx + kMaxStride) : s.ck_t;
+  s.basis = L.ckpt ? reinterpret_cast<float*>(s.tmp_idx + kMaxStride) : s.ck_t;
   s.col = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(s.basis + 12) + 15) & ~(uintptr_t)15);
   return s;
 }
@@ -723,6 +772,7 @@ template <int BD, typename ShT, int TR, int SS>
 __device__ __forceinline__ void run_colours(int nR, bool have_prev, const WarpSmem& sm, const float basis[9],
                                             const ShT* __restrict__ sh, int lane) {
   constexpr int C = 3 * BD;
+  constexpr int RS = row_stride32(C);
   // lane r-1 plans run r
   unsigned need = 0;
   int delta = 0;
@@ -741,8 +791,8 @@ __device__ __forceinline__ void run_colours(int nR, bool have_prev, const WarpSm
         delta = 4 * dx + 2 * dy + dz;
       }
     }
-    sm.run_need[r] = (int)need;
-    sm.run_delta[r] = delta;
+    sm.run_need[r] = (unsigned char)need;
+    sm.run_delta[r] = (signed char)delta;
   }
   // row table: exclusive prefix of the rows each run gathers
   const int cnt = __popc(need);
@@ -774,7 +824,7 @@ __device__ __forceinline__ void run_colours(int nR, bool have_prev, const WarpSm
       if (lane < C) {
         for (int u = 0; u < nrow; ++u) {
           const int lk = sm.rowlink[m0 + u];
-          cp_async4(sm.tile + u * C + lane, sh + (long long)(lk >= 0 ? lk : 0) * C + lane, lk >= 0 ? 4 : 0);
+          cp_async4(sm.tile + u * RS + lane, sh + (long long)(lk >= 0 ? lk : 0) * C + lane, lk >= 0 ? 4 : 0);
         }
         cp_async_wait_all();
       }
@@ -804,14 +854,21 @@ __device__ __forceinline__ void run_colours(int nR, bool have_prev, const WarpSm
       const int dst = sm.rowdst[m0 + lane];
       float* out = sm.slot + (dst >> 3) * SS + (dst & 7) * 3;
       if constexpr (std::is_same<ShT, float>::value) {
-        const float* row = sm.tile + lane * C;
+        // the row as float4 words (RS / 4 shared loads instead of C)
+        const float2* row4 = reinterpret_cast<const float2*>(sm.tile + lane * RS);
+        float acc[3] = {0.f, 0.f, 0.f};
 #pragma unroll
-        for (int gg = 0; gg < 3; ++gg) {
-          float acc = 0.f;
+        for (int w = 0; w < (C + 1) / 2; ++w) {
+          const float2 v = row4[w];
+          const float e[2] = {v.x, v.y};
 #pragma unroll
-          for (int k = 0; k < BD; ++k) acc = fmaf(basis[k], row[gg * BD + k], acc);
-          out[gg] = acc;
+          for (int i = 0; i < 2; ++i) {
+            const int k = 2 * w + i;
+            if (k < C) acc[k / BD] = fmaf(basis[k % BD], e[i], acc[k / BD]);
+          }
         }
+#pragma unroll
+        for (int gg = 0; gg < 3; ++gg) out[gg] = acc[gg];
       } else {
         const int lk = sm.rowlink[m0 + lane];
         // the table starts on a 4-byte boundary, so a row's half-word parity is that of lk * C
@@ -1393,15 +1450,13 @@ __device__ __forceinline__ void bg_backward(const BgArgs& b, float lt, float g0,
 
 // ---------------------------------------------------------------- kernel
 
-// The adjoint modes that keep segment checkpoints in shared memory (the two-kernel step needs
-// none: its reverse kernel reads every evaluated sample from the record), and the blocks per SM
-// each mode is compiled for: six (80 registers) for the forward kernels, seven (72 registers,
-// 76 bytes spilled, 2.3% faster than six) for the two-kernel step's reverse, four (128
-// registers) for the one-kernel adjoint.  Those with the MSI background or of the batch launch
-// keep five (96 registers): at 80 they spill, and the background's forward was 3% slower at six.
-__host__ __device__ constexpr bool ck_in_smem(int mode) { return mode == kFused || mode == kBwd; }
+// The blocks per SM each mode is compiled for: six (80 registers) for the forward kernels, eight
+// (64 registers, 84 bytes spilled; 1.2% faster than seven at 72 registers) for the two-kernel
+// step's reverse, four (128 registers) for the one-kernel adjoint.  Those with the MSI background
+// or of the batch launch keep five (96 registers): at 80 they spill, and the background's forward
+// was 3% slower at six.
 __host__ __device__ constexpr int blocks_per_sm_bound(int mode, bool multi, bool bg) {
-  if (mode == kFwd || mode == kFusedFwd || mode == kFusedRev) return multi || bg ? 5 : mode == kFusedRev ? 7 : 6;
+  if (mode == kFwd || mode == kFusedFwd || mode == kFusedRev) return multi || bg ? 5 : mode == kFusedRev ? 8 : 6;
   return kAdjointBlocksPerSm;
 }
 
@@ -1425,9 +1480,10 @@ __global__ void __launch_bounds__(kThreads, blocks_per_sm_bound(MODE, MULTI, BG)
   const int scap = (io.gcol != nullptr || kSplit) ? 0 : io.cap;  // samples in the shared-memory cache
   constexpr int TR = tile_rows<ShT, MODE>();
   constexpr int SS = slot_stride(MODE);
-  float* wbase = reinterpret_cast<float*>(smem4) +
-                 (size_t)wib * warp_smem_floats(C, scap, ck_in_smem(MODE), TR, SS, has_walk(MODE));
-  const WarpSmem sm = carve(wbase, C, scap, ck_in_smem(MODE), TR, SS, has_walk(MODE));
+  constexpr int FC = flush_cap(MODE);
+  const SmemLayout lay = smem_layout<ShT, MODE>(C, scap);
+  float* wbase = reinterpret_cast<float*>(smem4) + (size_t)wib * warp_smem_floats(lay);
+  const WarpSmem sm = carve(wbase, lay);
   const long long gslot = (long long)blockIdx.x * kWarps + wib;
   const bool gown = io.gcol != nullptr && gslot < io.gcol_warps;
   // one float4 per evaluated sample: its colour (before the +0.5 offset) and the log
@@ -1765,7 +1821,7 @@ __global__ void __launch_bounds__(kThreads, blocks_per_sm_bound(MODE, MULTI, BG)
         __syncwarp();
         // walk the runs last to first: merge shared corners, list the others, flush the list
         float* fl_val = sm.tile;
-        int* fl_link = reinterpret_cast<int*>(sm.tile + kFlushCap * 4);
+        int* fl_link = reinterpret_cast<int*>(sm.tile + FC * 4);
         int F = 0;
         walk_info(nR, have_b, bcell, sm, lane);
         for (int q = nR; q >= 1; --q) {
@@ -1774,7 +1830,7 @@ __global__ void __launch_bounds__(kThreads, blocks_per_sm_bound(MODE, MULTI, BG)
             // old corners not shared with the new cell (those on the faces it moved across) retire
             const unsigned retire = (unsigned)info & 0xFFu;
             if (retire) {
-              if (F + 8 > kFlushCap) {
+              if (F + 8 > FC) {
                 if (go.accum != nullptr)
                   flush_list_vec<BD>(F, fl_val, fl_link, sm.basis, go.accum, go.accum_stride, go.mask, lane);
                 else
@@ -1859,7 +1915,7 @@ __global__ void __launch_bounds__(kThreads, blocks_per_sm_bound(MODE, MULTI, BG)
       }
       if (have_b) {
         float* fl_val = sm.tile;
-        int* fl_link = reinterpret_cast<int*>(sm.tile + kFlushCap * 4);
+        int* fl_link = reinterpret_cast<int*>(sm.tile + FC * 4);
         list_retiring(0xFFu, B, lk_lane, fl_val, fl_link, 0, lane);
         if (go.accum != nullptr)
           flush_list_vec<BD>(8, fl_val, fl_link, sm.basis, go.accum, go.accum_stride, go.mask, lane);
@@ -1887,11 +1943,11 @@ int launch_t(const GridP& g, const OptP& opt, IoP io, long long n_rays, cudaStre
   const int cap = MODE == kFwd ? 0 : io.cap;
   io.cap = cap;
   if (MODE == kFwd) io.gcol = nullptr;
-  const size_t smem = sizeof(float) *
-                      (size_t)warp_smem_floats(C, (io.gcol != nullptr || MODE == kFusedFwd || MODE == kFusedRev) ? 0 : cap,
-                                               ck_in_smem(MODE), tile_rows<ShT, MODE>(), slot_stride(MODE),
-                                               has_walk(MODE)) *
-                      kWarps;
+  const size_t smem =
+      sizeof(float) *
+      (size_t)warp_smem_floats(
+          smem_layout<ShT, MODE>(C, (io.gcol != nullptr || MODE == kFusedFwd || MODE == kFusedRev) ? 0 : cap)) *
+      kWarps;
   // The function's dynamic shared-memory limit is one attribute per device for every
   // configuration (colour cache in shared or global memory, its capacity), so it is only ever
   // raised, to the largest configuration launched so far; the occupancy each configuration

@@ -307,14 +307,19 @@ __host__ __device__ constexpr bool ck_in_smem(int mode) { return mode == kFused 
 
 // Coefficient rows gathered per pass.  Rows are copied into shared memory with cp.async, all rows
 // of a pass in flight at once (one memory round trip per pass, no registers held): 32 rows for
-// the adjoint instantiations.  The forward ones take 12 FP32 rows (30 floats each) or 24 16-bit
-// rows (14 words each): their six blocks per SM then fit the 196 KB shared-memory carve-out and
-// leave 60 KB of the SM's 256 KB to L1, which holds the link and density gathers (FP32 forward
-// 7% faster than with 23 rows and 28 KB of L1).  The reverse kernel of the two-kernel fused step
-// gathers no rows (its colours are in the records): 0, and no row tables.
-template <typename ShT, int MODE>
+// the adjoint instantiations.  The forward ones at six blocks per SM take 12 FP32 rows (30 floats
+// each) or 24 16-bit rows (14 words each): their blocks then fit the 196 KB shared-memory
+// carve-out and leave 60 KB of the SM's 256 KB to L1, which holds the link and density gathers
+// (FP32 forward 7% faster than with 23 rows and 28 KB of L1).  At five blocks per SM (the MSI
+// background's and the batch launch's forward, five: true) 24 FP32 rows fit the same carve-out,
+// and fewer passes per segment count for more with fewer warps to hide them.  The reverse kernel
+// of the two-kernel fused step gathers no rows (its colours are in the records): 0, and no row
+// tables.
+template <typename ShT, int MODE, bool five = false>
 __host__ __device__ constexpr int tile_rows() {
-  return (MODE == kFwd || MODE == kFusedFwd) ? (std::is_same<ShT, float>::value ? 12 : 24) : MODE == kFusedRev ? 0 : 32;
+  return (MODE == kFwd || MODE == kFusedFwd) ? (std::is_same<ShT, float>::value && !five ? 12 : 24)
+         : MODE == kFusedRev                 ? 0
+                                             : 32;
 }
 
 // 4-byte words a 16-bit row of C coefficients can span (it starts on a 2-byte boundary).
@@ -386,9 +391,9 @@ struct SmemLayout {
   bool pc;    // the optical depths of the forward kernels' march
 };
 
-template <typename ShT, int MODE>
+template <typename ShT, int MODE, bool five>
 __host__ __device__ constexpr SmemLayout smem_layout(int C, int cap) {
-  return SmemLayout{tile_row_floats<ShT>(C), tile_rows<ShT, MODE>(), flush_cap(MODE), slot_stride(MODE), cap,
+  return SmemLayout{tile_row_floats<ShT>(C), tile_rows<ShT, MODE, five>(), flush_cap(MODE), slot_stride(MODE), cap,
                     ck_in_smem(MODE), has_walk(MODE), MODE != kFusedRev, MODE == kFwd || MODE == kFusedFwd};
 }
 
@@ -1478,10 +1483,10 @@ __global__ void __launch_bounds__(kThreads, blocks_per_sm_bound(MODE, MULTI, BG)
   // the ray's record (two-kernel step), or, without either, cap samples in shared memory.
   // Samples past the capacity are gathered again.
   const int scap = (io.gcol != nullptr || kSplit) ? 0 : io.cap;  // samples in the shared-memory cache
-  constexpr int TR = tile_rows<ShT, MODE>();
+  constexpr int TR = tile_rows<ShT, MODE, MULTI || BG>();
   constexpr int SS = slot_stride(MODE);
   constexpr int FC = flush_cap(MODE);
-  const SmemLayout lay = smem_layout<ShT, MODE>(C, scap);
+  const SmemLayout lay = smem_layout<ShT, MODE, MULTI || BG>(C, scap);
   float* wbase = reinterpret_cast<float*>(smem4) + (size_t)wib * warp_smem_floats(lay);
   const WarpSmem sm = carve(wbase, lay);
   const long long gslot = (long long)blockIdx.x * kWarps + wib;
@@ -1946,7 +1951,7 @@ int launch_t(const GridP& g, const OptP& opt, IoP io, long long n_rays, cudaStre
   const size_t smem =
       sizeof(float) *
       (size_t)warp_smem_floats(
-          smem_layout<ShT, MODE>(C, (io.gcol != nullptr || MODE == kFusedFwd || MODE == kFusedRev) ? 0 : cap)) *
+          smem_layout<ShT, MODE, MULTI || BG>(C, (io.gcol != nullptr || MODE == kFusedFwd || MODE == kFusedRev) ? 0 : cap)) *
       kWarps;
   // The function's dynamic shared-memory limit is one attribute per device for every
   // configuration (colour cache in shared or global memory, its capacity), so it is only ever

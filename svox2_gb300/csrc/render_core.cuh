@@ -1468,9 +1468,9 @@ __host__ __device__ constexpr int blocks_per_sm_bound(int mode, bool multi, bool
 template <int BD, typename ShT, int MODE, bool IMAGE, bool MULTI, bool BG = false>
 // 128 registers and 13.8 KB of shared memory per warp (SH9) let four blocks (16 warps) of the
 // one-kernel fused step share an SM; the march is latency-bound, so resident warps count for
-// more than the registers a larger budget would save.  The forward-only kernel and the two
-// kernels of the two-kernel fused step (no colour cache in shared memory; the forward keeps no
-// checkpoints there, the reverse gathers no rows) fit five blocks at 102 registers.
+// more than the registers a larger budget would save.  The forward kernels and the two-kernel
+// step's reverse (no colour cache in shared memory; the forward keeps no checkpoints there, the
+// reverse gathers no rows) fit the blocks blocks_per_sm_bound gives them.
 __global__ void __launch_bounds__(kThreads, blocks_per_sm_bound(MODE, MULTI, BG)) render_kernel(GridP g0, OptP opt,
                                                                                          IoP io) {
   constexpr int C = 3 * BD;

@@ -311,11 +311,11 @@ __host__ __device__ constexpr bool ck_in_smem(int mode) { return mode == kFused 
 // each) or 24 16-bit rows (14 words each): their blocks then fit the 196 KB shared-memory
 // carve-out and leave 60 KB of the SM's 256 KB to L1, which holds the row copies and gathers in
 // flight (FP32 forward 7% faster than with 23 rows and 28 KB of L1; the same 12-row layout
-// padded into the 228 KB carve-out is 12% slower, with more memory-pipe stalls).  At five blocks per SM (the MSI
-// background's and the batch launch's forward, five: true) 24 FP32 rows fit the same carve-out,
-// and fewer passes per segment count for more with fewer warps to hide them.  The reverse kernel
-// of the two-kernel fused step gathers no rows (its colours are in the records): 0, and no row
-// tables.
+// padded into the 228 KB carve-out is 12% slower, with more memory-pipe stalls).  At five blocks
+// per SM (the MSI background's and the batch launch's forward, five: true) 24 FP32 rows fit the
+// same carve-out, and fewer passes per segment count for more with fewer warps to hide them.
+// The reverse kernel of the two-kernel fused step gathers no rows (its colours are in the
+// records): 0, and no row tables.
 template <typename ShT, int MODE, bool five = false>
 __host__ __device__ constexpr int tile_rows() {
   return (MODE == kFwd || MODE == kFusedFwd) ? (std::is_same<ShT, float>::value && !five ? 12 : 24)

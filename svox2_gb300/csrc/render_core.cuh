@@ -404,7 +404,7 @@ __host__ __device__ constexpr int warp_smem_floats(const SmemLayout& L) {
           (L.ckpt ? 3 * kNumCkpt + 3 * kMaxStride : 0) + 16 + 4 * L.cap + 3) & ~3;
 }
 
-__device__ __forceinline__ WarpSmem carve(float* base, const SmemLayout& L) {
+__host__ __device__ __forceinline__ WarpSmem carve(float* base, const SmemLayout& L) {
   WarpSmem s;
   const int nrow = L.rows > 0 ? kMaxRows : 0;
   // the tile first: the warp's base is 16-byte aligned (warp_smem_floats is a multiple of 4)
